@@ -1,0 +1,264 @@
+/*
+ * nbh.h — C ABI of the GB300 Barnes-Hut step engine (libnbh.so).
+ *
+ * This is the drop-in boundary for the reference's per-step pipeline
+ * (bounding box -> octree build -> summarize -> sort -> force -> integrate).
+ * In the reference that pipeline is driven by the Java class
+ * GPUBarnesHutNBodySimulation through JOCL; here a Java FFM/JNI shim or Python
+ * ctypes drives it through the plain-C entry points below.  Every entry point
+ * takes plain pointers and sizes, returns an int status (0 = ok, negative =
+ * one of the NBH_ERR_* codes) and never throws.  One nbh_sim is not
+ * thread-safe; different nbh_sim objects may be used from different threads.
+ *
+ * Reference interfaces replaced (paths relative to the reference project):
+ *   AbstractNBodySimulation.java:16-43          step()/init()/getNumberOfBodies()
+ *   GPUBarnesHutNBodySimulation.java:104-151    constructor + init()
+ *   GPUBarnesHutNBodySimulation.java:153-181    loadBuffers()   (host -> device)
+ *   GPUBarnesHutNBodySimulation.java:219-227    calculateNumberOfNodes()
+ *   GPUBarnesHutNBodySimulation.java:229-246    initGLBuffers() (headless here)
+ *   GPUBarnesHutNBodySimulation.java:248-275    step() / executeSimulationKernel()
+ *   GPUBarnesHutNBodySimulation.java:276-290    error-flag read
+ *   GPUBarnesHutNBodySimulation.java:305-365    printEnergy/printDepth/printImpulse
+ *   universe/UniverseGenerator.java:22           generate(offset, n, x..m)
+ */
+#ifndef NBH_H
+#define NBH_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NBH_ABI_VERSION 1
+
+/* Status codes. */
+#define NBH_OK            0
+#define NBH_ERR_INVALID  (-1)  /* bad argument (null pointer, n<1, non-finite input, ...) */
+#define NBH_ERR_CUDA     (-2)  /* a CUDA runtime call failed; see nbh_last_error_message */
+#define NBH_ERR_POOL     (-3)  /* node pool exhausted while splitting cells
+                                  (reference: *_error = 1, buildtree.cl:112-119) */
+#define NBH_ERR_DEPTH    (-4)  /* tree deeper than NBH_MAXDEPTH levels
+                                  (reference: calculateforce.cl:69-73) */
+#define NBH_ERR_TIMEOUT  (-5)  /* a bounded device-side wait gave up (no reference
+                                  counterpart: the reference spins forever) */
+#define NBH_ERR_STATE    (-6)  /* call made in the wrong state (e.g. step before load) */
+#define NBH_ERR_NOMEM    (-7)  /* device allocation failed */
+#define NBH_ERR_NODEVICE (-8)  /* no CUDA device / wrong architecture */
+#define NBH_ERR_MODEL    (-9)  /* learned-theta model missing or malformed */
+
+/* Maximum tree depth (reference MAXDEPTH, calculateforce.cl:12). */
+#define NBH_MAXDEPTH 64
+
+/* Arithmetic modes of the step.
+ * NBH_ARITH_FMA       fused multiply-add where a*b+c occurs (default, fastest);
+ *                     inverse square root by the hardware approximation.
+ * NBH_ARITH_REFERENCE separate multiply and add, correctly rounded 1/sqrt:
+ *                     the arithmetic the reference kernels perform when the
+ *                     OpenCL compiler does not contract (-cl-mad-enable is a
+ *                     permission, GPUBarnesHutNBodySimulation.java:210). */
+#define NBH_ARITH_FMA       0
+#define NBH_ARITH_REFERENCE 1
+
+/* Run-time replacement of the reference's compile-time constants
+ * (calculateforce.cl:11-18, integrate.cl:11-12, GPUBarnesHutNBodySimulation.java:44-49,207-227). */
+typedef struct nbh_config {
+    int32_t abi_version;   /* must be NBH_ABI_VERSION */
+    int32_t device;        /* CUDA device ordinal */
+    float   theta;         /* opening angle; the reference's THETA macro is theta^2 */
+    float   eps;           /* softening length; the reference's EPSILON macro is eps^2 */
+    float   dt;            /* time step (TIMESTEP) */
+    float   G;             /* gravitational constant, multiplies every mass (reference: 1) */
+    float   pool_factor;   /* node pool = max(pool_factor*N, 16384) rounded up to 16;
+                              the reference uses 2.0 (calculateNumberOfNodes) */
+    int32_t vote_width;    /* bodies voting together on opening a cell: 32 (one warp,
+                              default) or 16 (the reference work-group, calculateforce.cl:145) */
+    int32_t arith;         /* NBH_ARITH_FMA or NBH_ARITH_REFERENCE */
+    int32_t precise;       /* 1: Kahan-compensated position/velocity updates and FP64
+                              extent / root centre of mass; 0: reference arithmetic */
+    int32_t stage_timing;  /* 1: record per-stage CUDA-event times in nbh_stats */
+    int32_t use_graph;     /* 1: replay each step as one captured CUDA graph (default) */
+    int32_t reserved[8];
+} nbh_config;
+
+/* Fills *cfg with the defaults: theta 0.5, eps 0.05, dt 0.025, G 1, pool 2.0,
+ * vote 32, FMA arithmetic, precise 0, stage timing 0, graph 1. */
+void nbh_config_default(nbh_config* cfg);
+
+typedef struct nbh_stats {
+    int64_t steps;             /* steps taken since the last load */
+    int64_t interactions;      /* accepted body-node force evaluations in the last step
+                                  (executions of calculateforce.cl:146-151) */
+    int32_t max_depth;         /* deepest level of the last tree (reference _maxDepth) */
+    int32_t cells;             /* cells allocated in the last tree, all universes */
+    int32_t nuniverses;
+    int32_t nbodies;           /* total over universes */
+    int32_t pool_nodes;        /* NUMBER_OF_NODES of the shared pool */
+    int32_t status;            /* device status word of the last step (NBH_OK or NBH_ERR_*) */
+    /* per-stage device milliseconds of the last step (stage_timing = 1 only) */
+    float   ms_bbox, ms_build, ms_summarize, ms_sort, ms_force, ms_integrate, ms_step;
+    float   reserved[8];
+} nbh_stats;
+
+typedef struct nbh_sim nbh_sim;
+
+/* Constructor (GPUBarnesHutNBodySimulation.java:104-108 + the device part of init :110-131). */
+int nbh_create(const nbh_config* cfg, nbh_sim** out);
+int nbh_destroy(nbh_sim* sim);
+
+/* Copies one universe of n bodies (SoA host arrays, like UniverseGenerator.generate's
+ * outputs) to the device and resets the step counter to -1 and max depth to 1, as
+ * loadBuffers does (GPUBarnesHutNBodySimulation.java:153-181).  Any pointer among
+ * vx, vy, vz may be NULL (zero velocity). */
+int nbh_load(nbh_sim* sim, int32_t n,
+             const float* x, const float* y, const float* z,
+             const float* vx, const float* vy, const float* vz,
+             const float* m);
+
+/* Batched ensemble: nuniv independent universes, universe u holding counts[u] bodies,
+ * stored back to back in the SoA arrays.  Every step advances all of them. */
+int nbh_load_batch(nbh_sim* sim, int32_t nuniv, const int32_t* counts,
+                   const float* x, const float* y, const float* z,
+                   const float* vx, const float* vy, const float* vz,
+                   const float* m);
+
+/* Runs nsteps full steps (BB -> build -> summarize -> sort -> force -> integrate) and
+ * waits for them, like step() (GPUBarnesHutNBodySimulation.java:248-271).  Returns the
+ * device status word (NBH_ERR_POOL / NBH_ERR_DEPTH / NBH_ERR_TIMEOUT) if a stage failed;
+ * stages after a failed one do nothing. */
+int nbh_step(nbh_sim* sim, int32_t nsteps);
+
+/* Enqueues nsteps steps on the sim's stream without waiting (no status check). */
+int nbh_step_async(nbh_sim* sim, int32_t nsteps);
+int nbh_synchronize(nbh_sim* sim);
+
+/* Reads the body state back (bodies in load order).  Any pointer may be NULL. */
+int nbh_read(nbh_sim* sim, float* x, float* y, float* z,
+             float* vx, float* vy, float* vz,
+             float* ax, float* ay, float* az);
+
+/* Overwrites positions, velocities and (optionally) accelerations without resetting the
+ * step counter: resume from a checkpoint, or a host that owns the arrays between steps.
+ * NULL pointers leave that component unchanged. */
+int nbh_write(nbh_sim* sim, const float* x, const float* y, const float* z,
+              const float* vx, const float* vy, const float* vz,
+              const float* ax, const float* ay, const float* az);
+
+int nbh_get_stats(nbh_sim* sim, nbh_stats* out);
+int32_t nbh_get_number_of_bodies(nbh_sim* sim);   /* getNumberOfBodies(), :376-379 */
+
+/* Headless stand-in for initGLBuffers + copyVertices (copyvertices.cl:8-17): writes
+ * float4 (x,y,z,1) and (vx,vy,vz,1) for every body into caller-owned DEVICE buffers of
+ * 4*N floats each (either may be NULL). */
+int nbh_export_float4(nbh_sim* sim, float* dev_pos4, float* dev_vel4);
+
+/* Last error text of this sim (or of the last failed nbh_create when sim is NULL). */
+const char* nbh_last_error_message(nbh_sim* sim);
+int nbh_last_error(nbh_sim* sim);
+
+/* Reference pool sizing (calculateNumberOfNodes, GPUBarnesHutNBodySimulation.java:219-227),
+ * generalised by pool_factor (2.0 reproduces the reference). */
+int32_t nbh_number_of_nodes(int32_t n, float pool_factor);
+
+/* ---- Tree inspection (tests and diagnostics) ------------------------------------ */
+
+/* Copies the last tree: child slots of every node index [0, pool_nodes] as int32[8*(pool_nodes+1)],
+ * node x,y,z,mass (centre of mass after summarize) as float[4*(pool_nodes+1)],
+ * body count and start per node as int32[pool_nodes+1], the sorted body order int32[N],
+ * and per-universe root node indices int32[nuniv] and root half-widths float[nuniv].
+ * Any pointer may be NULL. */
+int nbh_read_tree(nbh_sim* sim, int32_t* child, float* node4, int32_t* count,
+                  int32_t* start, int32_t* sorted, int32_t* roots, float* radius,
+                  int32_t* bottom);
+
+/* ---- Diagnostics (printEnergy / printImpulse, GPUBarnesHutNBodySimulation.java:305-365) */
+
+/* Kinetic energy, potential energy (each pair counted once, unlike the reference's
+ * printEnergy, which adds 2*e per pair at :334) and momentum, in FP64, over universe u
+ * (u = -1: all bodies as one system).  The potential uses the softened kernel
+ * -m_i m_j / sqrt(r^2 + eps^2) when softened != 0, the reference's bare 1/r otherwise. */
+int nbh_energy(nbh_sim* sim, int32_t u, int32_t softened,
+               double* kinetic, double* potential, double* momentum3);
+
+/* FP64 direct-sum accelerations of the bodies listed in idx (universe-global body
+ * indices), over all bodies of each listed body's own universe, with the sim's softening
+ * and G.  Output arrays hold nidx doubles each.  Used to measure force error. */
+int nbh_direct_f64(nbh_sim* sim, int32_t nidx, const int32_t* idx,
+                   double* ax, double* ay, double* az);
+
+/* ---- Learned per-body opening angle (no counterpart in the reference) ---------------- */
+
+/* Installs an MLP 12->64->64->1 (row-major fp32 weights: W1[64][12], b1[64], W2[64][64],
+ * b2[64], W3[64], b3[1]; 4993 floats) and the feature normalisation (mean[12], inv_std[12])
+ * that sets a per-body theta in [theta_min, theta_max]; BF16 weights are derived on the
+ * device.  enable = 0 returns to fixed theta. */
+int nbh_set_theta_model(nbh_sim* sim, const float* params, int32_t nparams,
+                        const float* feat_mean, const float* feat_inv_std,
+                        float theta_min, float theta_max, int32_t enable);
+
+/* Writes the 12 features of every body for the current tree into feat[N*12] (host). */
+int nbh_theta_features(nbh_sim* sim, float* feat);
+
+/* Writes the per-body theta used by the last step into theta[N] (host). */
+int nbh_read_theta(nbh_sim* sim, float* theta);
+
+/* One force evaluation on the current tree with a caller-given per-body theta (host
+ * array, N floats; NULL = the configured fixed theta), leaving positions and velocities
+ * untouched.  Accelerations are written to ax/ay/az (host, N floats each) and the number
+ * of interactions to *interactions.  Training data for the learned model come from this. */
+int nbh_force_probe(nbh_sim* sim, const float* theta_body,
+                    float* ax, float* ay, float* az, int64_t* interactions);
+
+/* ---- Seeded universe generators (UniverseGenerator implementations) ------------------ */
+/* All fill caller arrays of n floats at offset `offset`, deterministic in `seed`.
+ * Velocity pointers may be NULL where a generator leaves velocities unset. */
+
+/* Uniform in the ball of radius `radius`, Gaussian velocities of standard deviation
+ * vsigma, masses 1/n. */
+int nbh_generate_uniform_ball(uint64_t seed, int32_t offset, int32_t n, float radius, float vsigma,
+                              float* x, float* y, float* z, float* vx, float* vy, float* vz, float* m);
+/* Plummer sphere, scale radius a, total mass M, velocities from the distribution function
+ * (PlummerUniverseGenerator.java:6-43 without the 3*pi/16 rescale). */
+int nbh_generate_plummer(uint64_t seed, int32_t offset, int32_t n, float a, float M,
+                         float* x, float* y, float* z, float* vx, float* vy, float* vz, float* m);
+/* Exponential disc (scale length rd, scale height zd) with near-circular velocities, a
+ * central point mass mc (body `offset`) and a Plummer halo holding halo_frac of the
+ * particles, total mass 1 + mc. */
+int nbh_generate_disc(uint64_t seed, int32_t offset, int32_t n, float rd, float zd, float mc,
+                      float halo_frac,
+                      float* x, float* y, float* z, float* vx, float* vy, float* vz, float* m);
+/* RandomCubicUniverseGenerator.java:12-18: positions uniform in [-range/2, range/2)^3,
+ * masses 1/n, velocities untouched. */
+int nbh_generate_random_cube(uint64_t seed, int32_t offset, int32_t n, float range,
+                             float* x, float* y, float* z, float* m);
+/* SphericalUniverseGenerator.java:6-20: uniform on the unit sphere, masses 1/n. */
+int nbh_generate_sphere_surface(uint64_t seed, int32_t offset, int32_t n,
+                                float* x, float* y, float* z, float* m);
+/* MonteCarloSphericalUniverseGenerator.java:6-27: Fibonacci sphere with a seeded phase. */
+int nbh_generate_fibonacci_sphere(uint64_t seed, int32_t offset, int32_t n,
+                                  float* x, float* y, float* z, float* m);
+/* LonLatSphericalUniverseGenerator.java:9-29: radius 5 lon/lat sphere, masses 1/n. */
+int nbh_generate_lonlat_sphere(uint64_t seed, int32_t offset, int32_t n,
+                               float* x, float* y, float* z, float* m);
+/* RotatingDiskGalaxyGenerator.java:17-43: flat disc of radius r, centre mass at index
+ * offset, orbital speeds scaled by vmul. */
+int nbh_generate_rotating_disk(uint64_t seed, int32_t offset, int32_t n, float r, float vmul,
+                               float center_mass,
+                               float* x, float* y, float* z, float* vx, float* vy, float* vz,
+                               float* m);
+
+/* ---- .universe files (universe/serialize/*.java) ---------------------------------- */
+/* Java-serialisation stream: writeInt(n) then seven float[] objects x,y,z,vx,vy,vz,m
+ * (UniverseSerializer.java:25-34, SerializedUniverseGenerator.java:21-37).
+ * nbh_universe_read with x == NULL only reports *n. */
+int nbh_universe_read(const char* path, int32_t* n, float* x, float* y, float* z,
+                      float* vx, float* vy, float* vz, float* m);
+int nbh_universe_write(const char* path, int32_t n, const float* x, const float* y,
+                       const float* z, const float* vx, const float* vy, const float* vz,
+                       const float* m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NBH_H */
