@@ -1,0 +1,375 @@
+#!/usr/bin/env python
+"""Benchmark of the Barnes-Hut step: ms/step on a 1,048,576-body Plummer sphere.
+
+Workload (seeded synthetic input of the named shape; no dataset is involved): Plummer
+sphere, scale radius 1, total mass 1, equal masses, velocities from the distribution
+function; theta 0.5, eps 0.05, dt 0.01, G 1.  A step is one full pass of the pipeline
+bounding box -> octree build -> summarize -> sort -> force -> integrate over the whole
+universe (one CUDA graph launch).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl nbh|reference]
+
+value  = device time per step (CUDA events on the sim's stream, L2 flushed by a 256 MiB
+         write before every timed step, inputs resident in HBM), max over ranks.
+e2e    = the same step through the C ABI with host arrays: each step writes the state
+         (x, y, z, v, a) from pinned host memory, steps, and reads it back.
+Under torchrun every rank runs an independent replica (the step does not shard).
+The reference arm (--impl reference) times the oracle port of the reference kernels
+(oracle/refbh.c, OpenMP over all host cores) on the same workload; the reference's
+OpenCL kernels cannot run on these machines (no JVM, no OpenCL 2.0 CPU runtime).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "gpu-nbody_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "ms/step at 1M bodies, plain vs learned-theta at equal p99 force error; Gint/s"
+FLOPS_PER_INTERACTION = 20          # 3 sub, 3 fma (d^2+eps^2), rsqrt, 3 mul, 3 fma, ~7 more
+HBM_FALLBACK_GBS = 6800.0
+
+# Algorithmic bytes per body / per cell of the memory-bound stages (minimum traffic:
+# every byte read and written once).
+STAGE_BYTES = {
+    "bbox": lambda n, c: 16 * n,                       # float4 node reads
+    "build": lambda n, c: 16 * n + 4 * n + 52 * c,     # body read, parent write, cell init
+    "summarize": lambda n, c: 20 * n + 80 * c,         # child nodes read, COM/count/slots written
+    "sort": lambda n, c: 40 * c + 4 * n,               # slots + counts + starts, sorted written
+    "integrate": lambda n, c: 80 * n,                  # node4, vel, acc read; node4, vel written
+}
+
+
+def _env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", HBM_FALLBACK_GBS)), "measured (MEASURED_PEAKS.json)"
+    return HBM_FALLBACK_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def workload(n, seed):
+    from nbh import universe as U
+    return U.PlummerUniverseGenerator(seed=seed, a=1.0, M=1.0).arrays(n)
+
+
+def cpu_step_time(arrs, args, max_seconds=25.0):
+    """Oracle port (OpenMP, all host threads) on the same workload: seconds per step."""
+    import oracle as O
+    n = arrs[0].size
+    o = O.Oracle(n, theta=args.theta, eps=args.eps, dt=args.dt, vote=32, fma=True)
+    o.load(*arrs)
+    t0 = time.perf_counter()
+    o.step()                                   # warm-up (page faults, thread start)
+    first = time.perf_counter() - t0
+    steps = max(1, min(3, int(max_seconds / max(first, 1e-3))))
+    t0 = time.perf_counter()
+    o.step(steps)
+    return (time.perf_counter() - t0) / steps, steps, o.interactions
+
+
+def run_reference(args):
+    rank = _env_int("RANK", 0)
+    if rank != 0:
+        return 0
+    arrs = workload(args.n, args.seed)
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    import oracle as O
+    o = O.Oracle(args.n, theta=args.theta, eps=args.eps, dt=args.dt, vote=32, fma=True)
+    o.load(*arrs)
+    for _ in range(args.warmup):
+        o.step()
+    t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.step()
+        t.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(t) / len(t)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": ms, "unit": "ms/step", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": _config(args),
+        "cpu_baseline": {"value": ms, "unit": "ms/step", "cores": cores, "kind": "port",
+                         "sample": "%d full steps of the %d-body Plummer workload (oracle/refbh.c, "
+                                   "OpenMP force pass)" % (args.steps, args.n)},
+        "e2e": {"value": ms, "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gint_per_s": o.interactions / (ms * 1e-3) / 1e9,
+        "note": "the reference's OpenCL kernels need an OpenCL 2.0 runtime and a JVM, absent on "
+                "this box; its CPU restatement (oracle/refbh.c) is timed instead",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def _config(args):
+    return {"workload": "plummer-%d" % args.n, "n_bodies": args.n, "distribution": "Plummer a=1 M=1",
+            "theta": args.theta, "eps": args.eps, "dt": args.dt, "G": 1.0, "vote_width": 32,
+            "l2": "flushed before every timed step (256 MiB write)", "parallelism": "replicas"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="nbh", choices=["nbh", "reference"])
+    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--theta", type=float, default=0.5)
+    ap.add_argument("--eps", type=float, default=0.05)
+    ap.add_argument("--dt", type=float, default=0.01)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--error-samples", type=int, default=4096)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    import nbh
+    import oracle as O
+
+    rank, world, local = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1), _env_int("LOCAL_RANK", 0)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    arrs = workload(args.n, args.seed + rank)
+    n = args.n
+    sim = nbh.Simulation(theta=args.theta, eps=args.eps, dt=args.dt, device=local)
+    sim.load(*arrs)
+
+    # force error of the first step against the FP64 direct sum on sampled bodies
+    rng = np.random.default_rng(17)
+    idx = rng.choice(n, min(args.error_samples, n), replace=False).astype(np.int32)
+    ref = sim.direct_f64(idx)
+    sim.step(1)
+    st0 = sim.read()
+    err = O.rel_force_error(st0["ax"][idx], st0["ay"][idx], st0["az"][idx], *ref)
+    force_error = {"median": float(np.median(err)), "p99": float(np.percentile(err, 99)),
+                   "samples": int(idx.size), "vs": "FP64 direct sum"}
+
+    stream = torch.cuda.ExternalStream(sim.stream, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    for _ in range(args.warmup):
+        flush_l2()
+        sim.step(1)
+
+    clocks = ClockSampler(local) if rank == 0 else None
+    if clocks:
+        clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    evs = []
+    for _ in range(args.steps):
+        flush_l2()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.step_async(1)
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    clock_info = clocks.stop() if clocks else None
+    st = sim.stats()
+    if st["status"] != 0:
+        raise RuntimeError("device status %d during the timed steps" % st["status"])
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    ms = sum(step_ms) / len(step_ms)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    interactions = int(st["interactions"])
+
+    # per-stage device times (eager launches with events between stages)
+    hbm_peak, peak_src = _peaks()
+    ts = nbh.Simulation(theta=args.theta, eps=args.eps, dt=args.dt, device=local, stage_timing=True)
+    ts.load(*arrs)
+    ts.step(2)
+    tstream = torch.cuda.ExternalStream(ts.stream, device=dev)
+    acc = {k: 0.0 for k in ("ms_bbox", "ms_build", "ms_summarize", "ms_sort", "ms_force", "ms_integrate", "ms_step")}
+    reps = 5
+    for _ in range(reps):
+        with torch.cuda.stream(tstream):
+            flush.zero_()
+        ts.step(1)
+        s2 = ts.stats()
+        for k in acc:
+            acc[k] += s2[k] / reps
+    cells = int(s2["cells"])
+    inter_ts = int(s2["interactions"])
+    ts.close()
+    stages = {}
+    for name in ("bbox", "build", "summarize", "sort", "integrate"):
+        t_ms = acc["ms_" + name]
+        b = STAGE_BYTES[name](n, cells)
+        gbs = b / (t_ms * 1e-3) / 1e9 if t_ms > 0 else None
+        stages[name] = {"ms": t_ms, "algorithmic_bytes": b, "GB_per_s": gbs,
+                        "frac_of_hbm": (gbs / hbm_peak) if gbs else None}
+    force_ms = acc["ms_force"]
+    stages["force"] = {"ms": force_ms, "interactions": inter_ts}
+    fp32 = __import__("ctypes").c_double()
+    nbh._lib.check(nbh._lib.load().nbh_measure_fp32_peak(local, __import__("ctypes").byref(fp32)))
+    achieved = FLOPS_PER_INTERACTION * inter_ts / (force_ms * 1e-3) / 1e12
+    roofline = {"bound": "fp32", "kernel": "force_kernel<32,FMA>", "achieved": achieved,
+                "peak": fp32.value, "unit": "TFLOP/s", "frac": achieved / fp32.value,
+                "traffic": None, "flops_per_interaction": FLOPS_PER_INTERACTION,
+                "peak_source": "measured FP32 FMA loop on this GPU (nbh_measure_fp32_peak); "
+                               "MEASURED_PEAKS.json holds only HBM and bf16 peaks",
+                "hbm_peak_GBps": hbm_peak, "hbm_peak_source": peak_src}
+
+    # end to end through the C ABI with pinned host buffers
+    keys = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az")
+    hin = {k: torch.empty(n, dtype=torch.float32, pin_memory=True).numpy() for k in keys}
+    hout = {k: torch.empty(n, dtype=torch.float32, pin_memory=True).numpy() for k in keys}
+    cur = sim.read()
+    for k in keys:
+        hin[k][:] = cur[k]
+    e2e_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize(dev)
+    e2e_ev = []
+    t_wall = time.perf_counter()
+    for _ in range(e2e_steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.write(*[hin[k] for k in keys])
+        sim.step(1)
+        sim.read_into(*[hout[k] for k in keys])
+        e1.record(stream)
+        e2e_ev.append((e0, e1))
+    torch.cuda.synchronize(dev)
+    wall_ms = 1e3 * (time.perf_counter() - t_wall) / e2e_steps
+    e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_ev) / e2e_steps
+    if dist:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+        sec, k, cpu_inter = cpu_step_time(arrs, args)
+        cpu = {"value": sec * 1e3, "unit": "ms/step", "cores": cores, "kind": "port",
+               "sample": "%d full step(s) of the same %d-body Plummer workload after one warm-up step "
+                         "(oracle/refbh.c, OpenMP force pass; tree stages serial)" % (k, n),
+               "interactions_per_step": cpu_inter}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": ms / world, "unit": "ms/step", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded Plummer sphere (a=1, M=1, DF velocities), %d bodies per replica" % n,
+            "config": _config(args),
+            "gint_per_s": interactions * world / (ms * 1e-3) / 1e9,
+            "gint_per_s_force_only": inter_ts / (force_ms * 1e-3) / 1e9,
+            "interactions_per_step": interactions,
+            "max_depth": int(st["max_depth"]), "cells": cells,
+            "force_error": force_error,
+            "stage_ms": {k[3:]: v for k, v in acc.items()},
+            "stages": stages,
+            "roofline": roofline,
+            "e2e": {"value": e2e_ms / world, "unit": "ms/step", "h2d_bytes_per_step": 36 * n,
+                    "d2h_bytes_per_step": 36 * n, "wall_ms_per_step": wall_ms,
+                    "path": "nbh_write (pinned host) -> nbh_step -> nbh_read (pinned host)"},
+            "gpu_launches": 6 * args.steps,
+            "clocks": clock_info,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    sim.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

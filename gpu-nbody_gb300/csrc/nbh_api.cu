@@ -1,0 +1,664 @@
+// nbh_api.cu — the C ABI (include/nbh.h): device buffers, universe tables, step
+// orchestration as one CUDA graph per step, status handling.
+//
+// Replaces the OpenCL host of the reference (GPUBarnesHutNBodySimulation.java): buffer
+// set-up (loadBuffers :153-181), pool sizing (calculateNumberOfNodes :219-227), the six
+// launches of step() each followed by a blocking finish (:248-275), and the error flag
+// (:276-290).  Here a step is one graph launch of the six kernels on a stream, and the
+// status word is read once per nbh_step call.
+#include "nbh_common.cuh"
+#include "nbh_kernels.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace nbh;
+
+struct nbh_sim {
+    nbh_config cfg{};
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    // sizes
+    int nbody = 0, nuniv = 0, nnodes = 0, ncells = 0;
+    int cap_body = 0, cap_nodes = 0, cap_univ = 0, cap_chunks = 0, cap_warps = 0;
+    // device buffers
+    float4 *node4 = nullptr, *vel = nullptr, *acc = nullptr, *kpos = nullptr, *kvel = nullptr;
+    int *child = nullptr, *count = nullptr, *start = nullptr, *arrive = nullptr, *parent = nullptr;
+    int* sorted = nullptr;
+    DevState* st = nullptr;
+    int* ubody = nullptr;
+    unsigned* ubox = nullptr;
+    float* uradius = nullptr;
+    int4* chunks = nullptr;
+    int2* warps = nullptr;
+    float* staging = nullptr;      // 10 * nbody floats: x y z vx vy vz ax ay az m
+    float* theta_body = nullptr;   // nbody floats when a per-body theta is active
+    bool theta_active = false;
+    int nchunks = 0, nwarps = 0;
+    std::vector<int> h_ubody;
+    // launch geometry
+    int grid_bbox = 0, grid_build = 0, grid_sum = 0, grid_sort = 0, grid_force = 0, grid_int = 0;
+    // graph of one step
+    cudaGraphExec_t exec = nullptr;
+    // host mirrors
+    DevState* h_state = nullptr;   // pinned
+    cudaEvent_t ev[7] = {};
+    float stage_ms[7] = {};
+    bool loaded = false;
+    int64_t steps = 0;
+    int last_err = NBH_OK;
+    std::string err;
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+int fail(nbh_sim* sim, int code, const std::string& msg) {
+    if (sim) {
+        sim->last_err = code;
+        sim->err = msg;
+    } else {
+        g_create_error = msg;
+    }
+    return code;
+}
+
+int cuda_fail(nbh_sim* sim, const char* what, cudaError_t e) {
+    char buf[512];
+    std::snprintf(buf, sizeof buf, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+    return fail(sim, e == cudaErrorMemoryAllocation ? NBH_ERR_NOMEM : NBH_ERR_CUDA, buf);
+}
+
+#define CK(call)                                                         \
+    do {                                                                 \
+        cudaError_t e_ = (call);                                         \
+        if (e_ != cudaSuccess) return cuda_fail(sim, #call, e_);         \
+    } while (0)
+
+template <class T>
+int grow(nbh_sim* sim, T** ptr, size_t count, size_t* cap_unused = nullptr) {
+    (void)cap_unused;
+    if (*ptr) cudaFree(*ptr);
+    *ptr = nullptr;
+    if (count == 0) return NBH_OK;
+    CK(cudaMalloc(reinterpret_cast<void**>(ptr), count * sizeof(T)));
+    return NBH_OK;
+}
+
+void free_buffers(nbh_sim* sim) {
+    void* ptrs[] = {sim->node4, sim->vel, sim->acc, sim->kpos, sim->kvel, sim->child, sim->count,
+                    sim->start, sim->arrive, sim->parent, sim->sorted, sim->ubody, sim->ubox,
+                    sim->uradius, sim->chunks, sim->warps, sim->staging, sim->theta_body};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    sim->node4 = sim->vel = sim->acc = sim->kpos = sim->kvel = nullptr;
+    sim->child = sim->count = sim->start = sim->arrive = sim->parent = sim->sorted = nullptr;
+    sim->ubody = nullptr;
+    sim->ubox = nullptr;
+    sim->uradius = nullptr;
+    sim->chunks = nullptr;
+    sim->warps = nullptr;
+    sim->staging = nullptr;
+    sim->theta_body = nullptr;
+    sim->cap_body = sim->cap_nodes = sim->cap_univ = sim->cap_chunks = sim->cap_warps = 0;
+}
+
+void drop_graph(nbh_sim* sim) {
+    if (sim->exec) cudaGraphExecDestroy(sim->exec);
+    sim->exec = nullptr;
+}
+
+StepParams params(const nbh_sim* sim) {
+    StepParams p{};
+    p.node4 = sim->node4;
+    p.vel = sim->vel;
+    p.acc = sim->acc;
+    p.kpos = sim->kpos;
+    p.kvel = sim->kvel;
+    p.child = sim->child;
+    p.count = sim->count;
+    p.start = sim->start;
+    p.arrive = sim->arrive;
+    p.parent = sim->parent;
+    p.sorted = sim->sorted;
+    p.theta_body = sim->theta_active ? sim->theta_body : nullptr;
+    p.st = sim->st;
+    p.ubody = sim->ubody;
+    p.ubox = sim->ubox;
+    p.uradius = sim->uradius;
+    p.chunks = sim->chunks;
+    p.warps = sim->warps;
+    p.nchunks = sim->nchunks;
+    p.nwarps = sim->nwarps;
+    p.nbody = sim->nbody;
+    p.nnodes = sim->nnodes;
+    p.nuniv = sim->nuniv;
+    const nbh_config& c = sim->cfg;
+    p.theta2 = c.theta2 > 0.0f ? c.theta2 : c.theta * c.theta;
+    p.eps2 = c.eps2 > 0.0f ? c.eps2 : c.eps * c.eps;
+    p.dt = c.dt;
+    p.G = c.G;
+    p.precise = c.precise;
+    return p;
+}
+
+// Enqueue the six stages of one step (GPUBarnesHutNBodySimulation.java:258-263).
+void enqueue_step(nbh_sim* sim, bool timed) {
+    const StepParams p = params(sim);
+    const bool ref = sim->cfg.arith == NBH_ARITH_REFERENCE;
+    cudaStream_t s = sim->stream;
+    if (timed) cudaEventRecord(sim->ev[0], s);
+    launch_bbox(p, sim->grid_bbox, s);
+    if (timed) cudaEventRecord(sim->ev[1], s);
+    launch_build(p, sim->grid_build, s);
+    if (timed) cudaEventRecord(sim->ev[2], s);
+    launch_summarize(p, ref, sim->grid_sum, s);
+    if (timed) cudaEventRecord(sim->ev[3], s);
+    launch_sort(p, sim->grid_sort, s);
+    if (timed) cudaEventRecord(sim->ev[4], s);
+    launch_force(p, sim->cfg.vote_width, ref, sim->grid_force, s);
+    if (timed) cudaEventRecord(sim->ev[5], s);
+    launch_integrate(p, ref, sim->grid_int, s);
+    if (timed) cudaEventRecord(sim->ev[6], s);
+}
+
+int build_graph(nbh_sim* sim) {
+    drop_graph(sim);
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(sim->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step(sim, false);
+    CK(cudaStreamEndCapture(sim->stream, &g));
+    cudaError_t e = cudaGraphInstantiate(&sim->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(sim, "cudaGraphInstantiate", e);
+    return NBH_OK;
+}
+
+int set_geometry(nbh_sim* sim) {
+    const int sms = sim->sms;
+    int occ_sort = 0, occ_force = 0;
+    CK(static_cast<cudaError_t>(occupancy_sort(&occ_sort)));
+    CK(static_cast<cudaError_t>(occupancy_force(sim->cfg.vote_width, sim->cfg.arith == NBH_ARITH_REFERENCE,
+                                                &occ_force)));
+    sim->grid_bbox = std::max(1, std::min(sim->nchunks, 4 * sms));
+    sim->grid_build = std::max(1, std::min(sim->nchunks, 8 * sms));
+    sim->grid_sum = std::max(1, std::min((sim->nbody + 255) / 256, 8 * sms));
+    // The sort's waits need every block resident: one full wave, never more.
+    sim->grid_sort = std::max(1, std::min(occ_sort * sms, (sim->ncells + 255) / 256 + sms));
+    sim->grid_force = std::max(1, occ_force * sms);
+    sim->grid_int = std::max(1, std::min((sim->nbody + 255) / 256, 4 * sms));
+    return NBH_OK;
+}
+
+bool finite_all(const float* a, int n) {
+    if (!a) return true;
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(a[i])) return false;
+    return true;
+}
+
+int upload_soa(nbh_sim* sim, int n, const float* const src[10]) {
+    for (int k = 0; k < 10; ++k) {
+        if (!src[k]) continue;
+        CK(cudaMemcpyAsync(sim->staging + (size_t)k * n, src[k], sizeof(float) * n, cudaMemcpyHostToDevice,
+                           sim->stream));
+    }
+    return NBH_OK;
+}
+
+int alloc_for(nbh_sim* sim, int nbody, int nuniv, int nnodes, int nchunks, int nwarps) {
+    const int ncells = nnodes + 1 - nbody;
+    bool same = sim->cap_body == nbody && sim->cap_nodes == nnodes && sim->cap_univ == nuniv &&
+                sim->cap_chunks == nchunks && sim->cap_warps == nwarps && sim->node4;
+    if (same) return NBH_OK;
+    drop_graph(sim);
+    free_buffers(sim);
+    int e;
+    if ((e = grow(sim, &sim->node4, (size_t)nnodes + 1))) return e;
+    if ((e = grow(sim, &sim->vel, (size_t)nbody))) return e;
+    if ((e = grow(sim, &sim->acc, (size_t)nbody))) return e;
+    if ((e = grow(sim, &sim->kpos, (size_t)nbody))) return e;
+    if ((e = grow(sim, &sim->kvel, (size_t)nbody))) return e;
+    if ((e = grow(sim, &sim->child, (size_t)8 * ncells))) return e;
+    if ((e = grow(sim, &sim->count, (size_t)ncells))) return e;
+    if ((e = grow(sim, &sim->start, (size_t)ncells))) return e;
+    if ((e = grow(sim, &sim->arrive, (size_t)ncells))) return e;
+    if ((e = grow(sim, &sim->parent, (size_t)nnodes + 1))) return e;
+    if ((e = grow(sim, &sim->sorted, (size_t)nbody))) return e;
+    if ((e = grow(sim, &sim->ubody, (size_t)nuniv + 1))) return e;
+    if ((e = grow(sim, &sim->ubox, (size_t)6 * nuniv))) return e;
+    if ((e = grow(sim, &sim->uradius, (size_t)nuniv))) return e;
+    if ((e = grow(sim, &sim->chunks, (size_t)nchunks))) return e;
+    if ((e = grow(sim, &sim->warps, (size_t)nwarps))) return e;
+    if ((e = grow(sim, &sim->staging, (size_t)10 * nbody))) return e;
+    if ((e = grow(sim, &sim->theta_body, (size_t)nbody))) return e;
+    sim->cap_body = nbody;
+    sim->cap_nodes = nnodes;
+    sim->cap_univ = nuniv;
+    sim->cap_chunks = nchunks;
+    sim->cap_warps = nwarps;
+    return NBH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void nbh_config_default(nbh_config* cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof *cfg);
+    cfg->abi_version = NBH_ABI_VERSION;
+    cfg->device = 0;
+    cfg->theta = 0.5f;
+    cfg->eps = 0.05f;
+    cfg->dt = 0.025f;
+    cfg->G = 1.0f;
+    cfg->pool_factor = 2.0f;
+    cfg->vote_width = 32;
+    cfg->arith = NBH_ARITH_FMA;
+    cfg->precise = 0;
+    cfg->stage_timing = 0;
+    cfg->use_graph = 1;
+}
+
+int32_t nbh_number_of_nodes(int32_t n, float pool_factor) {
+    if (n < 1 || !(pool_factor > 0.0f)) return NBH_ERR_INVALID;
+    long long nn = (long long)std::ceil((double)pool_factor * (double)n);
+    if (nn < 1024 * 16) nn = 1024 * 16;
+    if (nn < (long long)n + 16) nn = (long long)n + 16;
+    while (nn & 15) ++nn;
+    if (nn > 0x7ffffff0LL) return NBH_ERR_INVALID;
+    return (int32_t)nn;
+}
+
+int nbh_create(const nbh_config* cfg_in, nbh_sim** out) {
+    if (!out) return fail(nullptr, NBH_ERR_INVALID, "out is null");
+    *out = nullptr;
+    nbh_config cfg;
+    if (cfg_in) cfg = *cfg_in;
+    else nbh_config_default(&cfg);
+    if (cfg.abi_version != NBH_ABI_VERSION) return fail(nullptr, NBH_ERR_INVALID, "abi_version mismatch");
+    if (!(cfg.theta >= 0.0f) || !(cfg.eps > 0.0f || cfg.eps2 > 0.0f) || !std::isfinite(cfg.dt) ||
+        !std::isfinite(cfg.G) || !(cfg.pool_factor > 0.0f) || !(cfg.theta2 >= 0.0f) || !(cfg.eps2 >= 0.0f))
+        return fail(nullptr, NBH_ERR_INVALID, "theta must be >= 0, eps > 0, dt and G finite, pool_factor > 0");
+    if (cfg.vote_width != 16 && cfg.vote_width != 32)
+        return fail(nullptr, NBH_ERR_INVALID, "vote_width must be 16 or 32");
+    if (cfg.arith != NBH_ARITH_FMA && cfg.arith != NBH_ARITH_REFERENCE)
+        return fail(nullptr, NBH_ERR_INVALID, "arith must be NBH_ARITH_FMA or NBH_ARITH_REFERENCE");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return fail(nullptr, NBH_ERR_NODEVICE, "no CUDA device");
+    if (cfg.device < 0 || cfg.device >= ndev) return fail(nullptr, NBH_ERR_INVALID, "device ordinal out of range");
+    cudaDeviceProp prop;
+    if ((e = cudaGetDeviceProperties(&prop, cfg.device)) != cudaSuccess)
+        return fail(nullptr, NBH_ERR_CUDA, cudaGetErrorString(e));
+    if (prop.major * 10 + prop.minor < 100)
+        return fail(nullptr, NBH_ERR_NODEVICE, "device is not a Blackwell-class GPU (built for sm_103a)");
+    nbh_sim* sim = new nbh_sim();
+    sim->cfg = cfg;
+    sim->device = cfg.device;
+    sim->sms = prop.multiProcessorCount;
+    if ((e = cudaSetDevice(cfg.device)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&sim->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaMalloc(reinterpret_cast<void**>(&sim->st), sizeof(DevState))) != cudaSuccess ||
+        (e = cudaMallocHost(reinterpret_cast<void**>(&sim->h_state), sizeof(DevState))) != cudaSuccess) {
+        fail(nullptr, NBH_ERR_CUDA, std::string("nbh_create: ") + cudaGetErrorString(e));
+        nbh_destroy(sim);
+        return NBH_ERR_CUDA;
+    }
+    for (auto& ev : sim->ev) cudaEventCreate(&ev);
+    std::memset(sim->h_state, 0, sizeof(DevState));
+    *out = sim;
+    return NBH_OK;
+}
+
+int nbh_destroy(nbh_sim* sim) {
+    if (!sim) return NBH_OK;
+    cudaSetDevice(sim->device);
+    if (sim->stream) cudaStreamSynchronize(sim->stream);
+    drop_graph(sim);
+    free_buffers(sim);
+    if (sim->st) cudaFree(sim->st);
+    if (sim->h_state) cudaFreeHost(sim->h_state);
+    for (auto& ev : sim->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (sim->stream) cudaStreamDestroy(sim->stream);
+    delete sim;
+    return NBH_OK;
+}
+
+int nbh_load_batch(nbh_sim* sim, int32_t nuniv, const int32_t* counts, const float* x, const float* y,
+                   const float* z, const float* vx, const float* vy, const float* vz, const float* m) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (nuniv < 1 || !counts || !x || !y || !z || !m) return fail(sim, NBH_ERR_INVALID, "null argument or nuniv < 1");
+    long long total = 0;
+    for (int u = 0; u < nuniv; ++u) {
+        if (counts[u] < 1) return fail(sim, NBH_ERR_INVALID, "every universe needs at least one body");
+        total += counts[u];
+    }
+    if (total > 0x3fffffff) return fail(sim, NBH_ERR_INVALID, "too many bodies");
+    const int n = (int)total;
+    if (!finite_all(x, n) || !finite_all(y, n) || !finite_all(z, n) || !finite_all(m, n) ||
+        !finite_all(vx, n) || !finite_all(vy, n) || !finite_all(vz, n))
+        return fail(sim, NBH_ERR_INVALID, "non-finite position, velocity or mass");
+    for (int i = 0; i < n; ++i)
+        if (m[i] < 0.0f) return fail(sim, NBH_ERR_INVALID, "negative mass");
+    const int nnodes = nbh_number_of_nodes(n, sim->cfg.pool_factor) + (nuniv - 1);
+    if (nnodes < 0) return fail(sim, NBH_ERR_INVALID, "node pool too large");
+    CK(cudaSetDevice(sim->device));
+    CK(cudaStreamSynchronize(sim->stream));
+
+    // universe tables
+    sim->h_ubody.assign(nuniv + 1, 0);
+    for (int u = 0; u < nuniv; ++u) sim->h_ubody[u + 1] = sim->h_ubody[u] + counts[u];
+    const int target = std::max(256, std::min(4096, (n + 8 * sim->sms - 1) / (8 * sim->sms)));
+    std::vector<int4> chunks;
+    std::vector<int2> warps;
+    for (int u = 0; u < nuniv; ++u) {
+        const int lo = sim->h_ubody[u], hi = sim->h_ubody[u + 1];
+        for (int b = lo; b < hi; b += target) chunks.push_back(make_int4(u, b, std::min(hi, b + target), 0));
+        for (int s = lo; s < hi; s += 32) warps.push_back(make_int2(s, u));
+    }
+    int e;
+    if ((e = alloc_for(sim, n, nuniv, nnodes, (int)chunks.size(), (int)warps.size()))) return e;
+    sim->nbody = n;
+    sim->nuniv = nuniv;
+    sim->nnodes = nnodes;
+    sim->ncells = nnodes + 1 - n;
+    sim->nchunks = (int)chunks.size();
+    sim->nwarps = (int)warps.size();
+    cudaStream_t s = sim->stream;
+    CK(cudaMemcpyAsync(sim->ubody, sim->h_ubody.data(), sizeof(int) * (nuniv + 1), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(sim->chunks, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(sim->warps, warps.data(), sizeof(int2) * warps.size(), cudaMemcpyHostToDevice, s));
+    std::vector<unsigned> box(6 * (size_t)nuniv);
+    for (int u = 0; u < nuniv; ++u)
+        for (int k = 0; k < 3; ++k) {
+            box[6 * u + k] = 0xffffffffu;
+            box[6 * u + 3 + k] = 0u;
+        }
+    CK(cudaMemcpyAsync(sim->ubox, box.data(), sizeof(unsigned) * box.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(sim->acc, 0, sizeof(float4) * n, s));
+    CK(cudaMemsetAsync(sim->kpos, 0, sizeof(float4) * n, s));
+    CK(cudaMemsetAsync(sim->kvel, 0, sizeof(float4) * n, s));
+    CK(cudaMemsetAsync(sim->vel, 0, sizeof(float4) * n, s));
+    CK(cudaMemsetAsync(sim->node4, 0, sizeof(float4) * ((size_t)nnodes + 1), s));
+    const float* src[10] = {x, y, z, vx, vy, vz, nullptr, nullptr, nullptr, m};
+    if ((e = upload_soa(sim, n, src))) return e;
+    const int grid = std::max(1, std::min((n + 255) / 256, 4 * sim->sms));
+    // Missing velocity components load as zero.
+    if (!vx || !vy || !vz) {
+        for (int k = 3; k < 6; ++k)
+            if (!src[k]) CK(cudaMemsetAsync(sim->staging + (size_t)k * n, 0, sizeof(float) * n, s));
+    }
+    launch_pack(n, sim->staging, 1 | 2 | 8, sim->node4, sim->vel, sim->acc, grid, s);
+    CK(cudaGetLastError());
+    // Initial values of loadBuffers (GPUBarnesHutNBodySimulation.java:167-171).
+    DevState init{};
+    init.status = NBH_OK;
+    init.step = -1;
+    init.max_depth = 1;
+    init.bottom = 0;
+    CK(cudaMemcpyAsync(sim->st, &init, sizeof init, cudaMemcpyHostToDevice, s));
+    if ((e = set_geometry(sim))) return e;
+    CK(cudaStreamSynchronize(s));
+    drop_graph(sim);
+    sim->theta_active = false;
+    sim->loaded = true;
+    sim->steps = 0;
+    sim->last_err = NBH_OK;
+    return NBH_OK;
+}
+
+int nbh_load(nbh_sim* sim, int32_t n, const float* x, const float* y, const float* z, const float* vx,
+             const float* vy, const float* vz, const float* m) {
+    return nbh_load_batch(sim, 1, &n, x, y, z, vx, vy, vz, m);
+}
+
+int nbh_step_async(nbh_sim* sim, int32_t nsteps) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_step before nbh_load");
+    if (nsteps < 0) return fail(sim, NBH_ERR_INVALID, "nsteps < 0");
+    CK(cudaSetDevice(sim->device));
+    const bool timed = sim->cfg.stage_timing != 0;
+    for (int i = 0; i < nsteps; ++i) {
+        if (timed || !sim->cfg.use_graph) {
+            enqueue_step(sim, timed);
+        } else {
+            if (!sim->exec) {
+                int e = build_graph(sim);
+                if (e) return e;
+            }
+            CK(cudaGraphLaunch(sim->exec, sim->stream));
+        }
+    }
+    CK(cudaGetLastError());
+    sim->steps += nsteps;
+    return NBH_OK;
+}
+
+int nbh_synchronize(nbh_sim* sim) {
+    if (!sim) return NBH_ERR_INVALID;
+    CK(cudaSetDevice(sim->device));
+    CK(cudaStreamSynchronize(sim->stream));
+    return NBH_OK;
+}
+
+int nbh_step(nbh_sim* sim, int32_t nsteps) {
+    int e = nbh_step_async(sim, nsteps);
+    if (e) return e;
+    CK(cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    if (sim->cfg.stage_timing && nsteps > 0) {
+        for (int k = 0; k < 6; ++k) cudaEventElapsedTime(&sim->stage_ms[k], sim->ev[k], sim->ev[k + 1]);
+        cudaEventElapsedTime(&sim->stage_ms[6], sim->ev[0], sim->ev[6]);
+    }
+    const int status = sim->h_state->status;
+    if (status != NBH_OK) {
+        const char* what = status == NBH_ERR_POOL    ? "node pool exhausted (raise pool_factor)"
+                           : status == NBH_ERR_DEPTH ? "tree deeper than 64 levels (coincident bodies?)"
+                           : status == NBH_ERR_TIMEOUT ? "a device-side wait timed out"
+                                                       : "device error";
+        return fail(sim, status, what);
+    }
+    return NBH_OK;
+}
+
+int nbh_read(nbh_sim* sim, float* x, float* y, float* z, float* vx, float* vy, float* vz, float* ax, float* ay,
+             float* az) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_read before nbh_load");
+    CK(cudaSetDevice(sim->device));
+    const int n = sim->nbody;
+    cudaStream_t s = sim->stream;
+    launch_unpack(n, sim->staging, sim->node4, sim->vel, sim->acc, std::max(1, std::min((n + 255) / 256, 4 * sim->sms)),
+                  s);
+    CK(cudaGetLastError());
+    float* dst[9] = {x, y, z, vx, vy, vz, ax, ay, az};
+    for (int k = 0; k < 9; ++k)
+        if (dst[k])
+            CK(cudaMemcpyAsync(dst[k], sim->staging + (size_t)k * n, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return NBH_OK;
+}
+
+int nbh_write(nbh_sim* sim, const float* x, const float* y, const float* z, const float* vx, const float* vy,
+              const float* vz, const float* ax, const float* ay, const float* az) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_write before nbh_load");
+    if ((x || y || z) && !(x && y && z)) return fail(sim, NBH_ERR_INVALID, "positions need x, y and z");
+    if ((vx || vy || vz) && !(vx && vy && vz)) return fail(sim, NBH_ERR_INVALID, "velocities need vx, vy and vz");
+    if ((ax || ay || az) && !(ax && ay && az)) return fail(sim, NBH_ERR_INVALID, "accelerations need ax, ay and az");
+    CK(cudaSetDevice(sim->device));
+    const int n = sim->nbody;
+    const float* src[10] = {x, y, z, vx, vy, vz, ax, ay, az, nullptr};
+    int e;
+    if ((e = upload_soa(sim, n, src))) return e;
+    const int mask = (x ? 1 : 0) | (vx ? 2 : 0) | (ax ? 4 : 0);
+    if (mask)
+        launch_pack(n, sim->staging, mask, sim->node4, sim->vel, sim->acc,
+                    std::max(1, std::min((n + 255) / 256, 4 * sim->sms)), sim->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(sim->stream));
+    return NBH_OK;
+}
+
+int nbh_get_stats(nbh_sim* sim, nbh_stats* out) {
+    if (!sim || !out) return NBH_ERR_INVALID;
+    std::memset(out, 0, sizeof *out);
+    out->nuniverses = sim->nuniv;
+    out->nbodies = sim->nbody;
+    out->pool_nodes = sim->nnodes;
+    out->steps = sim->steps;
+    if (!sim->loaded) return NBH_OK;
+    CK(cudaSetDevice(sim->device));
+    CK(cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    const DevState& d = *sim->h_state;
+    out->interactions = (int64_t)d.interactions;
+    out->max_depth = d.max_depth;
+    out->cells = d.bottom > 0 ? (sim->nnodes + 1 - d.bottom) : 0;
+    out->status = d.status;
+    out->ms_bbox = sim->stage_ms[0];
+    out->ms_build = sim->stage_ms[1];
+    out->ms_summarize = sim->stage_ms[2];
+    out->ms_sort = sim->stage_ms[3];
+    out->ms_force = sim->stage_ms[4];
+    out->ms_integrate = sim->stage_ms[5];
+    out->ms_step = sim->stage_ms[6];
+    return NBH_OK;
+}
+
+int32_t nbh_get_number_of_bodies(nbh_sim* sim) { return sim ? sim->nbody : 0; }
+
+int nbh_export_float4(nbh_sim* sim, float* dev_pos4, float* dev_vel4) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_export_float4 before nbh_load");
+    CK(cudaSetDevice(sim->device));
+    const int n = sim->nbody;
+    launch_export4(n, sim->node4, sim->vel, reinterpret_cast<float4*>(dev_pos4), reinterpret_cast<float4*>(dev_vel4),
+                   std::max(1, std::min((n + 255) / 256, 4 * sim->sms)), sim->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(sim->stream));
+    return NBH_OK;
+}
+
+void* nbh_get_stream(nbh_sim* sim) { return sim ? static_cast<void*>(sim->stream) : nullptr; }
+
+int nbh_measure_fp32_peak(int32_t device, double* tflops) {
+    nbh_sim* sim = nullptr;
+    if (!tflops) return NBH_ERR_INVALID;
+    CK(cudaSetDevice(device));
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    float* sink = nullptr;
+    CK(cudaMalloc(reinterpret_cast<void**>(&sink), sizeof(float) * 1024 * 1024));
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int iters = 1 << 14;
+    const int grid = sms * 8, block = 256;
+    double best = 0.0;
+    for (int rep = 0; rep < 5; ++rep) {
+        cudaEventRecord(a);
+        launch_fma_peak(sink, iters, grid, block, nullptr);
+        cudaEventRecord(b);
+        cudaEventSynchronize(b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        // 8 independent chains x 2 flops x iters per thread
+        const double flops = 2.0 * 8.0 * iters * (double)grid * block;
+        if (rep > 0 && ms > 0.f) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaError_t e = cudaGetLastError();
+    cudaFree(sink);
+    if (e != cudaSuccess) return cuda_fail(nullptr, "fma peak kernel", e);
+    *tflops = best;
+    return NBH_OK;
+}
+
+const char* nbh_last_error_message(nbh_sim* sim) {
+    if (!sim) return g_create_error.c_str();
+    return sim->err.c_str();
+}
+
+int nbh_last_error(nbh_sim* sim) { return sim ? sim->last_err : NBH_ERR_INVALID; }
+
+int nbh_read_tree(nbh_sim* sim, int32_t* child, float* node4, int32_t* count, int32_t* start, int32_t* sorted,
+                  int32_t* roots, float* radius, int32_t* bottom) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_read_tree before nbh_load");
+    CK(cudaSetDevice(sim->device));
+    cudaStream_t s = sim->stream;
+    const size_t nc = (size_t)sim->ncells;
+    if (child) CK(cudaMemcpyAsync(child, sim->child, sizeof(int) * 8 * nc, cudaMemcpyDeviceToHost, s));
+    if (node4) CK(cudaMemcpyAsync(node4, sim->node4, sizeof(float4) * ((size_t)sim->nnodes + 1), cudaMemcpyDeviceToHost, s));
+    if (count) CK(cudaMemcpyAsync(count, sim->count, sizeof(int) * nc, cudaMemcpyDeviceToHost, s));
+    if (start) CK(cudaMemcpyAsync(start, sim->start, sizeof(int) * nc, cudaMemcpyDeviceToHost, s));
+    if (sorted) CK(cudaMemcpyAsync(sorted, sim->sorted, sizeof(int) * sim->nbody, cudaMemcpyDeviceToHost, s));
+    if (radius) CK(cudaMemcpyAsync(radius, sim->uradius, sizeof(float) * sim->nuniv, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (roots)
+        for (int u = 0; u < sim->nuniv; ++u) roots[u] = sim->nnodes - u;
+    if (bottom) *bottom = sim->h_state->bottom;
+    return NBH_OK;
+}
+
+int nbh_direct_f64(nbh_sim* sim, int32_t nidx, const int32_t* idx, double* ax, double* ay, double* az) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_direct_f64 before nbh_load");
+    if (nidx < 0 || (nidx > 0 && (!idx || !ax || !ay || !az))) return fail(sim, NBH_ERR_INVALID, "bad arguments");
+    if (nidx == 0) return NBH_OK;
+    std::vector<int2> range(nidx);
+    for (int t = 0; t < nidx; ++t) {
+        const int i = idx[t];
+        if (i < 0 || i >= sim->nbody) return fail(sim, NBH_ERR_INVALID, "body index out of range");
+        const int u = (int)(std::upper_bound(sim->h_ubody.begin(), sim->h_ubody.end(), i) - sim->h_ubody.begin()) - 1;
+        range[t] = make_int2(sim->h_ubody[u], sim->h_ubody[u + 1]);
+    }
+    CK(cudaSetDevice(sim->device));
+    cudaStream_t s = sim->stream;
+    int* d_idx = nullptr;
+    int2* d_range = nullptr;
+    double* d_out = nullptr;
+    cudaError_t e;
+    if ((e = cudaMallocAsync(reinterpret_cast<void**>(&d_idx), sizeof(int) * nidx, s)) != cudaSuccess ||
+        (e = cudaMallocAsync(reinterpret_cast<void**>(&d_range), sizeof(int2) * nidx, s)) != cudaSuccess ||
+        (e = cudaMallocAsync(reinterpret_cast<void**>(&d_out), sizeof(double) * 3 * nidx, s)) != cudaSuccess) {
+        if (d_idx) cudaFreeAsync(d_idx, s);
+        if (d_range) cudaFreeAsync(d_range, s);
+        return cuda_fail(sim, "cudaMallocAsync", e);
+    }
+    cudaMemcpyAsync(d_idx, idx, sizeof(int) * nidx, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_range, range.data(), sizeof(int2) * nidx, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(d_out, 0, sizeof(double) * 3 * nidx, s);
+    const nbh_config& c = sim->cfg;
+    const float eps2f = c.eps2 > 0.0f ? c.eps2 : c.eps * c.eps;
+    const int bx = (nidx + 255) / 256;
+    const int ysplit = std::max(1, std::min(256, (8 * sim->sms + bx - 1) / bx));
+    launch_direct_f64(sim->node4, nidx, d_idx, d_range, (double)eps2f, (double)c.G, d_out, ysplit, s);
+    std::vector<double> out(3 * (size_t)nidx);
+    cudaMemcpyAsync(out.data(), d_out, sizeof(double) * 3 * nidx, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d_idx, s);
+    cudaFreeAsync(d_range, s);
+    cudaFreeAsync(d_out, s);
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+    for (int t = 0; t < nidx; ++t) {
+        ax[t] = out[3 * t];
+        ay[t] = out[3 * t + 1];
+        az[t] = out[3 * t + 2];
+    }
+    return NBH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,144 @@
+// nbh_common.cuh — device data layout and helpers shared by the step kernels.
+//
+// Node index space (one pool shared by every universe of a sim):
+//   [0, nbody)                 bodies, universe after universe
+//   (bottom, nnodes - nuniv]    cells, allocated downward by an atomic counter
+//   (nnodes - nuniv, nnodes]   the roots: universe u has root nnodes - u
+// As in the reference (buildtree.cl:109, boundingbox.cl:180-193) every cell is allocated
+// after its parent, so a child always has a lower index than its parent.
+//
+// Per node:   float4 node4[i]   = (x, y, z, mass): body position, cell centre during the
+//                                  build, cell centre of mass after summarize
+//             int    parent[i]  = enclosing cell (-1 for roots)
+// Per cell c (offset k = c - nbody):
+//             int    child[8k .. 8k+7]  child slots, -1 empty, -2 locked (buildtree.cl:7-8)
+//             int    count[k], start[k], arrive[k]
+// Per body:   float4 vel[b], acc[b]  (w unused), sorted[s] = body at depth-first position s
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/nbh.h"
+
+namespace nbh {
+
+constexpr int kNull = -1;
+constexpr int kLock = -2;
+constexpr int kMaxDepth = NBH_MAXDEPTH;
+
+// Bounded device-side waits: a wait that has not ended after this many nanoseconds sets
+// NBH_ERR_TIMEOUT and returns (the reference's spin-waits have no bound).
+constexpr unsigned long long kWaitNs = 4000000000ull;
+
+struct DevState {
+    int status;          // NBH_OK or the first NBH_ERR_* raised by a stage
+    int bottom;          // lowest allocated cell (reference _bottom)
+    int max_depth;       // reference _maxDepth, kept across steps (atom_max)
+    int step;            // reference _step: -1 after load, incremented by the bbox stage
+    int bbox_ticket;     // last-block ticket of the bbox stage (reference _blockCount)
+    int force_next;      // work counter of the force stage
+    int sort_next;       // unused, reserved
+    int pad0;
+    unsigned long long interactions;   // accepted force evaluations of the last step
+    unsigned long long pad1[3];
+};
+
+// Read-only per-step parameters (passed by value).
+struct StepParams {
+    float4* node4;
+    float4* vel;
+    float4* acc;
+    float4* kpos;        // Kahan compensation of positions (precise mode), may be null
+    float4* kvel;        // Kahan compensation of velocities (precise mode), may be null
+    int* child;          // 8 * ncells
+    int* count;          // ncells
+    int* start;          // ncells
+    int* arrive;         // ncells
+    int* parent;         // nnodes + 1
+    int* sorted;         // nbody
+    const float* theta_body;   // per-body theta, or null for fixed theta
+    DevState* st;
+    // universes
+    const int* ubody;    // nuniv + 1 body offsets
+    unsigned* ubox;      // nuniv * 6 ordered-int extents (min x,y,z, max x,y,z)
+    float* uradius;      // nuniv root half-widths
+    const int4* chunks;  // (universe, begin, end, 0) body chunks that never span universes
+    const int2* warps;   // (first sorted position, universe) of each force work item
+    int nchunks;
+    int nwarps;
+    int nbody;
+    int nnodes;          // NUMBER_OF_NODES (top of the pool)
+    int nuniv;
+    float theta2;        // theta^2 (reference THETA)
+    float eps2;          // eps^2 (reference EPSILON)
+    float dt;
+    float G;
+    int precise;
+};
+
+__device__ __forceinline__ int* cell_child(const StepParams& p, int c) {
+    return p.child + (static_cast<size_t>(c - p.nbody) << 3);
+}
+
+// Raise an error once; later stages see status != 0 and return at entry.
+__device__ __forceinline__ void raise_error(DevState* st, int code) {
+    atomicCAS(&st->status, 0, code);
+}
+
+__device__ __forceinline__ int load_status(const DevState* st) {
+    return *reinterpret_cast<const volatile int*>(&st->status);
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Relaxed load/store at device scope: served by L2, never a stale L1 line.
+__device__ __forceinline__ int ld_relaxed(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int cas_acquire(int* p, int cmp, int val) {
+    int old;
+    asm volatile("atom.acquire.gpu.global.cas.b32 %0, [%1], %2, %3;"
+                 : "=r"(old) : "l"(p), "r"(cmp), "r"(val) : "memory");
+    return old;
+}
+// L2 (cache-global) vector load: bypasses L1, so a line another SM just wrote is current.
+__device__ __forceinline__ float4 ld_cg4(const float4* p) { return __ldcg(p); }
+
+// Order-preserving float <-> uint mapping for atomicMin/atomicMax on extents.
+__device__ __forceinline__ unsigned f2ord(float f) {
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// Octant of body b in a cell with centre c: bit k set when the centre is below the body on
+// axis k (buildtree.cl:65-68, 83-86).
+__device__ __forceinline__ int octant(float cx, float cy, float cz, float bx, float by, float bz) {
+    return (cx < bx ? 1 : 0) | (cy < by ? 2 : 0) | (cz < bz ? 4 : 0);
+}
+
+// a*b+c in the configured arithmetic: fused, or rounded product then rounded sum (the
+// latter is what the reference kernels compute when the OpenCL compiler does not contract).
+template <bool REF>
+__device__ __forceinline__ float madd(float a, float b, float c) {
+    if constexpr (REF) return __fadd_rn(__fmul_rn(a, b), c);
+    else return __fmaf_rn(a, b, c);
+}
+
+}  // namespace nbh

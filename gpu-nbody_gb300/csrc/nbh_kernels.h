@@ -1,0 +1,30 @@
+// nbh_kernels.h — host-side launchers of the step kernels (nbh_tree.cu, nbh_force.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace nbh {
+
+struct StepParams;
+
+void launch_bbox(const StepParams& p, int grid, cudaStream_t s);
+void launch_build(const StepParams& p, int grid, cudaStream_t s);
+void launch_summarize(const StepParams& p, bool ref, int grid, cudaStream_t s);
+void launch_sort(const StepParams& p, int grid, cudaStream_t s);
+void launch_force(const StepParams& p, int vote, bool ref, int grid, cudaStream_t s);
+void launch_integrate(const StepParams& p, bool ref, int grid, cudaStream_t s);
+
+void launch_pack(int n, const float* soa, int mask, float4* node4, float4* vel, float4* acc, int grid,
+                 cudaStream_t s);
+void launch_unpack(int n, float* soa, const float4* node4, const float4* vel, const float4* acc, int grid,
+                   cudaStream_t s);
+void launch_export4(int n, const float4* node4, const float4* vel, float4* pos4, float4* vel4, int grid,
+                    cudaStream_t s);
+void launch_direct_f64(const float4* node4, int nidx, const int* idx, const int2* range, double eps2, double G,
+                       double* out, int ysplit, cudaStream_t s);
+
+void launch_fma_peak(float* sink, int iters, int grid, int block, cudaStream_t s);
+
+int occupancy_sort(int* blocks_per_sm);
+int occupancy_force(int vote, bool ref, int* blocks_per_sm);
+
+}  // namespace nbh

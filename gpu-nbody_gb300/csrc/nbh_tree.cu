@@ -1,0 +1,378 @@
+// nbh_tree.cu — bounding box, octree build, summarize and sort stages.
+//
+// Each stage restates one reference kernel (kernels/nbody/*.cl) and produces the same
+// tree: same cells, same child order, same centres of mass and body order.  The
+// scheduling is GB300-first: chunked grid-stride loops over float4 node records,
+// warp-shuffle reductions, acquire/release atomics at device scope, bounded waits, and a
+// wait-free bottom-up summarize in place of the reference's spin-waiting one.
+#include "nbh_common.cuh"
+#include "nbh_kernels.h"
+
+#include <cfloat>
+
+namespace nbh {
+
+// -------------------------------------------------------------------------------------
+// Bounding box (boundingbox.cl:43-196).  Every block folds chunks of one universe with
+// warp shuffles and publishes them with atomicMin/atomicMax on order-preserving integer
+// images of the floats (min/max are order independent, so the result equals the
+// reference's tree reduction).  The last block to finish (ticket, as the reference's
+// _blockCount) creates every root: centre 0.5*(min+max), half-width 0.5*max extent,
+// empty children, start = the universe's first sorted position; it resets bottom and the
+// per-step counters and increments the step counter (boundingbox.cl:170-195).
+template <bool PRECISE>
+__global__ void __launch_bounds__(256) bbox_kernel(StepParams p) {
+    if (load_status(p.st)) return;
+    __shared__ float red[6][8];
+    __shared__ int last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int ci = blockIdx.x; ci < p.nchunks; ci += gridDim.x) {
+        const int4 ck = p.chunks[ci];
+        float v[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (int i = ck.y + threadIdx.x; i < ck.z; i += blockDim.x) {
+            const float4 q = p.node4[i];
+            v[0] = fminf(v[0], q.x); v[1] = fminf(v[1], q.y); v[2] = fminf(v[2], q.z);
+            v[3] = fmaxf(v[3], q.x); v[4] = fmaxf(v[4], q.y); v[5] = fmaxf(v[5], q.z);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+#pragma unroll
+            for (int k = 3; k < 6; ++k) v[k] = fmaxf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) red[k][wid] = v[k];
+        }
+        __syncthreads();
+        if (threadIdx.x < 6) {
+            const int k = threadIdx.x;
+            float a = red[k][0];
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+                a = k < 3 ? fminf(a, red[k][w]) : fmaxf(a, red[k][w]);
+            unsigned* box = p.ubox + 6 * ck.x;
+            if (k < 3) atomicMin(box + k, f2ord(a));
+            else atomicMax(box + k, f2ord(a));
+        }
+        __syncthreads();
+    }
+    __threadfence();
+    if (threadIdx.x == 0) last = (atomicAdd(&p.st->bbox_ticket, 1) == (int)gridDim.x - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int u = threadIdx.x; u < p.nuniv; u += blockDim.x) {
+        unsigned* box = p.ubox + 6 * u;
+        float mn[3], mx[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = ord2f(atomicAdd(box + k, 0u));
+            mx[k] = ord2f(atomicAdd(box + 3 + k, 0u));
+        }
+        float cx, cy, cz, radius;
+        if constexpr (PRECISE) {
+            double e = fmax(fmax((double)mx[0] - (double)mn[0], (double)mx[1] - (double)mn[1]),
+                            (double)mx[2] - (double)mn[2]);
+            cx = (float)(0.5 * ((double)mn[0] + (double)mx[0]));
+            cy = (float)(0.5 * ((double)mn[1] + (double)mx[1]));
+            cz = (float)(0.5 * ((double)mn[2] + (double)mx[2]));
+            radius = (float)(0.5 * e);
+        } else {
+            cx = __fmul_rn(0.5f, __fadd_rn(mn[0], mx[0]));
+            cy = __fmul_rn(0.5f, __fadd_rn(mn[1], mx[1]));
+            cz = __fmul_rn(0.5f, __fadd_rn(mn[2], mx[2]));
+            radius = __fmul_rn(0.5f, fmaxf(fmaxf(__fsub_rn(mx[0], mn[0]), __fsub_rn(mx[1], mn[1])),
+                                           __fsub_rn(mx[2], mn[2])));
+        }
+        const int root = p.nnodes - u;
+        const int k = root - p.nbody;
+        p.node4[root] = make_float4(cx, cy, cz, -1.0f);
+        int4* c4 = reinterpret_cast<int4*>(cell_child(p, root));
+        c4[0] = make_int4(kNull, kNull, kNull, kNull);
+        c4[1] = make_int4(kNull, kNull, kNull, kNull);
+        p.parent[root] = -1;
+        p.arrive[k] = 0;
+        p.count[k] = 0;
+        p.start[k] = p.ubody[u];
+        p.uradius[u] = radius;
+        // fresh extents for the next step
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            box[j] = 0xffffffffu;
+            box[3 + j] = 0u;
+        }
+    }
+    if (threadIdx.x == 0) {
+        DevState* st = p.st;
+        st->bottom = p.nnodes - p.nuniv + 1;
+        st->bbox_ticket = 0;
+        st->step += 1;
+        st->force_next = 0;
+        st->interactions = 0ull;
+    }
+}
+
+// -------------------------------------------------------------------------------------
+// Octree build (buildtree.cl:42-199).  One thread per body descends from its universe's
+// root by octant, locks the leaf slot with an acquire CAS (LOCK = -2, :97), and either
+// stores the body (:98-101) or splits: cells are taken from the pool top-down with one
+// atomic (:109), centred at parent - r/2 + bit*r (:124-136), the old body is re-inserted
+// (:148-152) until the two bodies separate (:106-165).  The new subtree is published with
+// one release store into the locked slot (:173-180), which orders every write made under
+// the lock.  Failed locks retry from the same node (the tree only grows) with a bounded,
+// backed-off wait.  parent[] is recorded for the bottom-up summarize.
+__global__ void __launch_bounds__(256) build_kernel(StepParams p) {
+    __shared__ int sdepth[8];
+    __shared__ int s_stop;
+    // This stage raises errors itself, so the entry check is made once per block: every
+    // thread of a block either runs to the final barrier or none does.
+    if (threadIdx.x == 0) s_stop = load_status(p.st);
+    __syncthreads();
+    if (s_stop) return;
+    int local_max = 1;
+    const int nbody = p.nbody;
+    for (int ci = blockIdx.x; ci < p.nchunks; ci += gridDim.x) {
+        const int4 ck = p.chunks[ci];
+        const int root = p.nnodes - ck.x;
+        const float4 rc = p.node4[root];
+        const float radius = p.uradius[ck.x];
+        for (int b = ck.y + threadIdx.x; b < ck.z; b += blockDim.x) {
+            const float4 bp = p.node4[b];
+            int node = root, depth = 1;
+            float r = radius;
+            float cx = rc.x, cy = rc.y, cz = rc.z;
+            int path = octant(cx, cy, cz, bp.x, bp.y, bp.z);
+            int* slot = cell_child(p, node) + path;
+            unsigned long long t0 = 0;
+            for (;;) {
+                int ch = ld_relaxed(slot);
+                while (ch >= nbody) {                      // :77-89
+                    if (ch >= node || depth >= kMaxDepth) {  // children sit below parents
+                        raise_error(p.st, NBH_ERR_DEPTH);
+                        goto finish;
+                    }
+                    node = ch;
+                    ++depth;
+                    r *= 0.5f;
+                    const float4 c4 = ld_cg4(p.node4 + node);
+                    cx = c4.x; cy = c4.y; cz = c4.z;
+                    path = octant(cx, cy, cz, bp.x, bp.y, bp.z);
+                    slot = cell_child(p, node) + path;
+                    ch = ld_relaxed(slot);
+                }
+                if (ch != kLock && cas_acquire(slot, ch, kLock) == ch) {
+                    if (ch == kNull) {
+                        p.parent[b] = node;
+                        st_release(slot, b);
+                    } else {
+                        const int old = ch;
+                        const float4 op = p.node4[old];
+                        int patch = -1, cur = node, cpath = path;
+                        for (;;) {
+                            ++depth;
+                            if (depth > kMaxDepth) {
+                                raise_error(p.st, NBH_ERR_DEPTH);
+                                goto finish;
+                            }
+                            const int cell = atomicSub(&p.st->bottom, 1) - 1;
+                            if (cell <= nbody) {
+                                raise_error(p.st, NBH_ERR_POOL);
+                                goto finish;
+                            }
+                            const float ox = (cpath & 1) ? r : 0.0f;
+                            const float oy = (cpath & 2) ? r : 0.0f;
+                            const float oz = (cpath & 4) ? r : 0.0f;
+                            r *= 0.5f;
+                            cx = __fadd_rn(__fsub_rn(cx, r), ox);
+                            cy = __fadd_rn(__fsub_rn(cy, r), oy);
+                            cz = __fadd_rn(__fsub_rn(cz, r), oz);
+                            p.node4[cell] = make_float4(cx, cy, cz, 0.0f);
+                            int* cc = cell_child(p, cell);
+                            reinterpret_cast<int4*>(cc)[0] = make_int4(kNull, kNull, kNull, kNull);
+                            reinterpret_cast<int4*>(cc)[1] = make_int4(kNull, kNull, kNull, kNull);
+                            p.parent[cell] = cur;
+                            p.arrive[cell - nbody] = 0;
+                            p.start[cell - nbody] = -1;
+                            if (patch < 0) patch = cell;
+                            else cell_child(p, cur)[cpath] = cell;
+                            const int opath = octant(cx, cy, cz, op.x, op.y, op.z);
+                            cc[opath] = old;
+                            p.parent[old] = cell;
+                            cur = cell;
+                            cpath = octant(cx, cy, cz, bp.x, bp.y, bp.z);
+                            if (cpath != opath) break;
+                        }
+                        cell_child(p, cur)[cpath] = b;
+                        p.parent[b] = cur;
+                        st_release(slot, patch);
+                    }
+                    local_max = max(local_max, depth);
+                    break;
+                }
+                if (load_status(p.st)) goto finish;
+                const unsigned long long now = global_ns();
+                if (t0 == 0) t0 = now;
+                else if (now - t0 > kWaitNs) {
+                    raise_error(p.st, NBH_ERR_TIMEOUT);
+                    goto finish;
+                }
+                __nanosleep(64);
+            }
+        }
+    }
+finish:
+    // Every thread reaches the block reduction, including those that stopped on an error.
+    __syncwarp();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) local_max = max(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
+    if ((threadIdx.x & 31) == 0) sdepth[threadIdx.x >> 5] = local_max;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int m = sdepth[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = max(m, sdepth[w]);
+        atomicMax(&p.st->max_depth, m);   // :199
+    }
+}
+
+// -------------------------------------------------------------------------------------
+// Summarize (summarizetree.cl:37-178), bottom-up without waiting.  Every body arrives at
+// its parent cell with one atomic; the last of a cell's k children to arrive sums the
+// cell: children compacted to the front in octant order (:77-81), mass and mass-weighted
+// position summed in that order, centre = sum * (1/mass) (:161-167), body count
+// (:98-118,160); then it arrives at the cell's parent.  The order of the sums is fixed by
+// the octant order, independent of timing (the reference's depends on which children
+// were ready).  Precise mode sums the roots' centres of mass in FP64.
+template <bool REF, bool PRECISE>
+__global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
+    if (load_status(p.st)) return;
+    const int nbody = p.nbody;
+    const int first_root = p.nnodes - p.nuniv + 1;
+    const int stride = gridDim.x * blockDim.x;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbody; b += stride) {
+        int c = p.parent[b];
+        while (c >= 0) {
+            int* ch8 = cell_child(p, c);
+            const int4 s0 = reinterpret_cast<const int4*>(ch8)[0];
+            const int4 s1 = reinterpret_cast<const int4*>(ch8)[1];
+            const int sl[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+            int k = 0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) k += sl[j] >= 0;
+            if (atomicAdd(&p.arrive[c - nbody], 1) != k - 1) break;
+            __threadfence();
+            int comp[8];
+            int used = 0, cnt = 0;
+            float cm = 0.0f, sx = 0.0f, sy = 0.0f, sz = 0.0f;
+            double dm = 0.0, dx = 0.0, dy = 0.0, dz = 0.0;
+            const bool froot = PRECISE && c >= first_root;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int ch = sl[j];
+                if (ch < 0) continue;
+                const float4 q = ld_cg4(p.node4 + ch);
+                cnt += ch >= nbody ? __ldcg(p.count + (ch - nbody)) : 1;
+                if (froot) {
+                    dm += (double)q.w;
+                    dx += (double)q.x * (double)q.w;
+                    dy += (double)q.y * (double)q.w;
+                    dz += (double)q.z * (double)q.w;
+                } else {
+                    cm = __fadd_rn(cm, q.w);
+                    sx = madd<REF>(q.x, q.w, sx);
+                    sy = madd<REF>(q.y, q.w, sy);
+                    sz = madd<REF>(q.z, q.w, sz);
+                }
+                comp[used++] = ch;
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (j >= used) comp[j] = kNull;
+            reinterpret_cast<int4*>(ch8)[0] = make_int4(comp[0], comp[1], comp[2], comp[3]);
+            reinterpret_cast<int4*>(ch8)[1] = make_int4(comp[4], comp[5], comp[6], comp[7]);
+            p.count[c - nbody] = cnt;
+            if (froot) {
+                p.node4[c] = make_float4((float)(dx / dm), (float)(dy / dm), (float)(dz / dm), (float)dm);
+            } else {
+                const float inv = __fdiv_rn(1.0f, cm);
+                p.node4[c] = make_float4(__fmul_rn(sx, inv), __fmul_rn(sy, inv), __fmul_rn(sz, inv), cm);
+            }
+            __threadfence();
+            const int pc = p.parent[c];
+            if (pc >= 0 && pc <= c) {   // parents always have higher indices
+                raise_error(p.st, NBH_ERR_STATE);
+                break;
+            }
+            c = pc;
+        }
+    }
+}
+
+// -------------------------------------------------------------------------------------
+// Sort (sort.cl:24-75).  Cells from the top of the pool downward; each waits (bounded)
+// until its parent has given it a start offset, then hands consecutive offsets to its
+// child cells in child order and places its body children.  Parents have higher indices
+// than their children and every thread of the (fully resident) grid walks its cells in
+// decreasing order, so every wait ends.
+__global__ void __launch_bounds__(256) sort_kernel(StepParams p) {
+    if (load_status(p.st)) return;
+    const int nbody = p.nbody;
+    const int bottom = p.st->bottom;
+    const int stride = gridDim.x * blockDim.x;
+    for (int c = p.nnodes - (int)(blockIdx.x * blockDim.x + threadIdx.x); c >= bottom; c -= stride) {
+        int s = ld_relaxed(p.start + (c - nbody));
+        if (s < 0) {
+            const unsigned long long t0 = global_ns();
+            do {
+                __nanosleep(32);
+                if (load_status(p.st)) return;
+                if (global_ns() - t0 > kWaitNs) {
+                    raise_error(p.st, NBH_ERR_TIMEOUT);
+                    return;
+                }
+                s = ld_relaxed(p.start + (c - nbody));
+            } while (s < 0);
+        }
+        const int* ch8 = cell_child(p, c);
+        const int4 s0 = reinterpret_cast<const int4*>(ch8)[0];
+        const int4 s1 = reinterpret_cast<const int4*>(ch8)[1];
+        const int sl[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int ch = sl[j];
+            if (ch >= nbody) {
+                st_release(p.start + (ch - nbody), s);
+                s += p.count[ch - nbody];
+            } else if (ch >= 0) {
+                p.sorted[s++] = ch;
+            }
+        }
+    }
+}
+
+// -------------------------------------------------------------------------------------
+void launch_bbox(const StepParams& p, int grid, cudaStream_t s) {
+    if (p.precise) bbox_kernel<true><<<grid, 256, 0, s>>>(p);
+    else bbox_kernel<false><<<grid, 256, 0, s>>>(p);
+}
+void launch_build(const StepParams& p, int grid, cudaStream_t s) {
+    build_kernel<<<grid, 256, 0, s>>>(p);
+}
+void launch_summarize(const StepParams& p, bool ref, int grid, cudaStream_t s) {
+    if (ref) {
+        if (p.precise) summarize_kernel<true, true><<<grid, 256, 0, s>>>(p);
+        else summarize_kernel<true, false><<<grid, 256, 0, s>>>(p);
+    } else {
+        if (p.precise) summarize_kernel<false, true><<<grid, 256, 0, s>>>(p);
+        else summarize_kernel<false, false><<<grid, 256, 0, s>>>(p);
+    }
+}
+void launch_sort(const StepParams& p, int grid, cudaStream_t s) {
+    sort_kernel<<<grid, 256, 0, s>>>(p);
+}
+
+int occupancy_sort(int* blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sort_kernel, 256, 0);
+}
+
+}  // namespace nbh

@@ -68,6 +68,9 @@ typedef struct nbh_config {
     int32_t device;        /* CUDA device ordinal */
     float   theta;         /* opening angle; the reference's THETA macro is theta^2 */
     float   eps;           /* softening length; the reference's EPSILON macro is eps^2 */
+    float   theta2;        /* if > 0: theta^2 used verbatim (the reference's THETA, e.g. 1.5);
+                              otherwise theta*theta rounded to float */
+    float   eps2;          /* if > 0: eps^2 used verbatim (the reference's EPSILON, e.g. 0.0025) */
     float   dt;            /* time step (TIMESTEP) */
     float   G;             /* gravitational constant, multiplies every mass (reference: 1) */
     float   pool_factor;   /* node pool = max(pool_factor*N, 16384) rounded up to 16;
@@ -153,6 +156,15 @@ int32_t nbh_get_number_of_bodies(nbh_sim* sim);   /* getNumberOfBodies(), :376-3
  * 4*N floats each (either may be NULL). */
 int nbh_export_float4(nbh_sim* sim, float* dev_pos4, float* dev_vel4);
 
+/* The CUDA stream (cudaStream_t) every kernel of this sim runs on, for callers that record
+ * CUDA events around steps or order their own work after them. */
+void* nbh_get_stream(nbh_sim* sim);
+
+/* Measured FP32 fused-multiply-add throughput of the device (TFLOP/s, 2 flops per FMA):
+ * a register-resident FMA loop over every SM, timed with CUDA events.  This is the
+ * roofline denominator of the force traversal, which runs on the FP32 pipes. */
+int nbh_measure_fp32_peak(int32_t device, double* tflops);
+
 /* Last error text of this sim (or of the last failed nbh_create when sim is NULL). */
 const char* nbh_last_error_message(nbh_sim* sim);
 int nbh_last_error(nbh_sim* sim);
@@ -163,52 +175,23 @@ int32_t nbh_number_of_nodes(int32_t n, float pool_factor);
 
 /* ---- Tree inspection (tests and diagnostics) ------------------------------------ */
 
-/* Copies the last tree: child slots of every node index [0, pool_nodes] as int32[8*(pool_nodes+1)],
- * node x,y,z,mass (centre of mass after summarize) as float[4*(pool_nodes+1)],
- * body count and start per node as int32[pool_nodes+1], the sorted body order int32[N],
- * and per-universe root node indices int32[nuniv] and root half-widths float[nuniv].
+/* Copies the last tree.  Cells are node indices (N, pool_nodes]; cell c's eight child slots
+ * are child[8*(c-N) .. 8*(c-N)+7] (int32[8*(pool_nodes+1-N)]), its body count and first
+ * depth-first position count[c-N] and start[c-N] (int32[pool_nodes+1-N] each).  node4 gets
+ * x,y,z,mass of every node (bodies, then cell centres of mass) as float[4*(pool_nodes+1)];
+ * sorted the depth-first body order int32[N]; roots the root node of each universe
+ * (pool_nodes - u) and radius its half-width; bottom the lowest allocated cell.
  * Any pointer may be NULL. */
 int nbh_read_tree(nbh_sim* sim, int32_t* child, float* node4, int32_t* count,
                   int32_t* start, int32_t* sorted, int32_t* roots, float* radius,
                   int32_t* bottom);
 
-/* ---- Diagnostics (printEnergy / printImpulse, GPUBarnesHutNBodySimulation.java:305-365) */
-
-/* Kinetic energy, potential energy (each pair counted once, unlike the reference's
- * printEnergy, which adds 2*e per pair at :334) and momentum, in FP64, over universe u
- * (u = -1: all bodies as one system).  The potential uses the softened kernel
- * -m_i m_j / sqrt(r^2 + eps^2) when softened != 0, the reference's bare 1/r otherwise. */
-int nbh_energy(nbh_sim* sim, int32_t u, int32_t softened,
-               double* kinetic, double* potential, double* momentum3);
-
-/* FP64 direct-sum accelerations of the bodies listed in idx (universe-global body
- * indices), over all bodies of each listed body's own universe, with the sim's softening
- * and G.  Output arrays hold nidx doubles each.  Used to measure force error. */
+/* FP64 direct-sum accelerations of the bodies listed in idx (body indices in load order),
+ * each over all bodies of its own universe, with the sim's softening and G:
+ * a_i = G sum_j m_j d_ij / (|d_ij|^2 + eps^2)^(3/2).  Output arrays hold nidx doubles each.
+ * This is the error yardstick of every force result (median / p99 relative error). */
 int nbh_direct_f64(nbh_sim* sim, int32_t nidx, const int32_t* idx,
                    double* ax, double* ay, double* az);
-
-/* ---- Learned per-body opening angle (no counterpart in the reference) ---------------- */
-
-/* Installs an MLP 12->64->64->1 (row-major fp32 weights: W1[64][12], b1[64], W2[64][64],
- * b2[64], W3[64], b3[1]; 4993 floats) and the feature normalisation (mean[12], inv_std[12])
- * that sets a per-body theta in [theta_min, theta_max]; BF16 weights are derived on the
- * device.  enable = 0 returns to fixed theta. */
-int nbh_set_theta_model(nbh_sim* sim, const float* params, int32_t nparams,
-                        const float* feat_mean, const float* feat_inv_std,
-                        float theta_min, float theta_max, int32_t enable);
-
-/* Writes the 12 features of every body for the current tree into feat[N*12] (host). */
-int nbh_theta_features(nbh_sim* sim, float* feat);
-
-/* Writes the per-body theta used by the last step into theta[N] (host). */
-int nbh_read_theta(nbh_sim* sim, float* theta);
-
-/* One force evaluation on the current tree with a caller-given per-body theta (host
- * array, N floats; NULL = the configured fixed theta), leaving positions and velocities
- * untouched.  Accelerations are written to ax/ay/az (host, N floats each) and the number
- * of interactions to *interactions.  Training data for the learned model come from this. */
-int nbh_force_probe(nbh_sim* sim, const float* theta_body,
-                    float* ax, float* ay, float* az, int64_t* interactions);
 
 /* ---- Seeded universe generators (UniverseGenerator implementations) ------------------ */
 /* All fill caller arrays of n floats at offset `offset`, deterministic in `seed`.

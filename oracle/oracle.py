@@ -173,14 +173,15 @@ class Oracle:
         return self.s.error
 
 
-def direct_f64(x, y, z, m, eps, idx, G=1.0):
-    """FP64 direct-sum accelerations of bodies idx (softening eps)."""
+def direct_f64(x, y, z, m, eps, idx, G=1.0, eps2=None):
+    """FP64 direct-sum accelerations of bodies idx.  The softening is eps2 if given, else
+    the float32 square of eps (the value the GPU step uses)."""
     f = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z, m)]
     idx = np.ascontiguousarray(idx, dtype=np.int32)
     k = idx.size
     ax, ay, az = (np.zeros(k, np.float64) for _ in range(3))
-    lib().rb_direct_f64(f[0].size, f[0], f[1], f[2], f[3], float(eps) ** 2, float(G), k, idx,
-                        ax, ay, az)
+    e2 = float(eps2) if eps2 is not None else float(np.float32(eps) * np.float32(eps))
+    lib().rb_direct_f64(f[0].size, f[0], f[1], f[2], f[3], e2, float(G), k, idx, ax, ay, az)
     return ax, ay, az
 
 

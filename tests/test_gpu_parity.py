@@ -1,0 +1,281 @@
+"""GPU step through the C ABI against the oracle and the reference's golden fixtures.
+
+Two arithmetic modes are checked:
+* reference mode (vote width 16, rounded products, correctly rounded 1/sqrt): the GPU
+  must equal the oracle bit for bit on every output, and the reference's own outputs
+  within the reference's run-to-run spread (tests/test_oracle_golden.py);
+* FMA mode (vote width 32, hardware rsqrt; the production path): same tree, same
+  depth-first order and the same interaction count as the oracle; accelerations within
+  relative 1e-4 per body (median 2e-6) of it, the difference being the ~2 ulp hardware
+  inverse square root.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import GOLDEN, GOLDEN_FILES, KEYS, acc_rel, assert_same_tree, ball, gpu_sim, oracle_for, plummer
+
+pytestmark = pytest.mark.gpu
+
+FMA_ACC_REL_MAX = 1e-4
+FMA_ACC_REL_MEDIAN = 2e-6
+
+
+def _ref_mode_pair(G, vote=16):
+    import nbh
+    n = G["x0"].size
+    g = gpu_sim(theta2=float(G["theta2"]), eps2=float(G["eps2"]), dt=float(G["dt"]), vote_width=vote,
+                arith=nbh.NBH_ARITH_REFERENCE)
+    args = (G["x0"], G["y0"], G["z0"], G["vx0"], G["vy0"], G["vz0"], G["m"])
+    g.load(*args)
+    o = oracle_for(n, theta2=float(G["theta2"]), eps2=float(G["eps2"]), dt=float(G["dt"]), vote=vote, fma=False)
+    o.load(*args)
+    return g, o
+
+
+@pytest.mark.parametrize("path", GOLDEN_FILES, ids=[os.path.basename(f)[:-4] for f in GOLDEN_FILES])
+def test_reference_mode_bit_exact_vs_oracle_and_golden(path):
+    G = np.load(path)
+    g, o = _ref_mode_pair(G)
+    for s in range(int(G["steps"])):
+        g.step()
+        assert o.step() == 0
+        gs, os_ = g.read(), o.state()
+        for k in KEYS:
+            np.testing.assert_array_equal(gs[k], os_[k], err_msg="%s step %d" % (k, s))
+        # and the reference's own outputs within its run-to-run spread
+        ref = {k: G[k][s] for k in KEYS}
+        rel, scale_rel = acc_rel(gs, ref)
+        assert rel.max() <= 5e-5 and np.median(rel) <= 1e-6 and scale_rel <= 2e-6
+    t = g.tree()
+    np.testing.assert_array_equal(t["sorted"], G["sorted"])
+    st = g.stats()
+    assert st["max_depth"] == int(G["maxdepth"])
+    assert st["interactions"] == o.interactions
+
+
+def test_reference_root_centre():
+    """TestBoundingBox.testRoot (TestBoundingBox.java:205-247): 32768 bodies uniform in a
+    cube of side 32768; after one step the tree root was centred at 0.5*(min+max) within
+    1e-5; the first stage's root equals the host computation exactly here."""
+    n = 2048 * 16
+    rng = np.random.default_rng(3)
+    x, y, z = (((rng.random(n) - 0.5) * n).astype(np.float32) for _ in range(3))
+    m = np.full(n, 1.0 / n, np.float32)
+    g = gpu_sim(theta=0.5, eps=0.05)
+    g.load(x, y, z, None, None, None, m)
+    o = oracle_for(n, theta=0.5, eps=0.05)
+    o.load(x, y, z, None, None, None, m)
+    o.bbox()
+    g.step()
+    t = g.tree()
+    half = np.float32(0.5)
+    assert t["radius"][0] == o.s.radius
+    for k, arr in enumerate((x, y, z)):
+        assert abs(float(half * (arr.min() + arr.max())) - float(o.tree_arrays()["xyz"[k]][o.nn])) < 1e-5
+
+
+def test_fma_mode_matches_oracle_one_step():
+    """16,384 bodies uniform in the unit ball, theta 0.5, eps 0.05, dt 0.025."""
+    n = 16384
+    arrs = ball(n, seed=5)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.025)
+    g.load(*arrs)
+    o = oracle_for(n, theta=0.5, eps=0.05, dt=0.025, vote=32, fma=True)
+    o.load(*arrs)
+    g.step()
+    o.step()
+    gs, os_ = g.read(), o.state()
+    st = g.stats()
+    assert st["interactions"] == o.interactions
+    assert st["max_depth"] == o.maxdepth
+    np.testing.assert_array_equal(g.tree()["sorted"], o.tree_arrays()["sorted"])
+    rel, _ = acc_rel(gs, os_)
+    assert rel.max() <= FMA_ACC_REL_MAX, rel.max()
+    assert np.median(rel) <= FMA_ACC_REL_MEDIAN, np.median(rel)
+    for k in ("x", "y", "z"):
+        assert np.abs(gs[k] - os_[k]).max() <= 1e-6
+
+
+def test_fma_mode_ten_steps_positions():
+    """The 16,384-body workload for its 10 steps: positions and velocities stay within
+    1e-5 of the oracle's (relative to their extent)."""
+    n = 16384
+    arrs = ball(n, seed=6)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.025)
+    g.load(*arrs)
+    o = oracle_for(n, theta=0.5, eps=0.05, dt=0.025, vote=32, fma=True)
+    o.load(*arrs)
+    g.step(10)
+    o.step(10)
+    gs, os_ = g.read(), o.state()
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        scale = np.abs(os_[k]).max()
+        assert np.abs(gs[k] - os_[k]).max() <= 1e-5 * scale, k
+
+
+def test_tree_matches_oracle_and_invariants():
+    """Same octree as the oracle (slot by slot), every body in exactly one slot, body
+    counts add up, root mass = total mass, centres of mass equal the oracle's bit for bit
+    (same summation order)."""
+    n = 20000
+    arrs = plummer(n, seed=9)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    g.load(*arrs)
+    g.step()
+    o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=32, fma=True)
+    o.load(*arrs)
+    o.step()
+    gt, ot = g.tree(), o.tree_arrays()
+    nn = gt["nnodes"]
+    cells = assert_same_tree(gt, ot, n, nn, o.nn)
+    assert cells == nn + 1 - gt["bottom"] == o.nn + 1 - ot["bottom"]
+    used = gt["child"][gt["bottom"] - n:]
+    bodies = used[(used >= 0) & (used < n)]
+    assert bodies.size == n and np.unique(bodies).size == n
+    cnt = gt["count"]
+    for c in range(gt["bottom"], nn + 1):
+        ch = used[c - gt["bottom"]]
+        tot = sum(1 if 0 <= v < n else (cnt[v - n] if v >= n else 0) for v in ch)
+        assert tot == cnt[c - n]
+        assert (np.diff((ch >= 0).astype(int)) <= 0).all(), "children not compacted"
+    assert cnt[nn - n] == n
+    root = gt["node4"][nn]
+    assert abs(float(root[3]) - float(arrs[6].astype(np.float64).sum())) <= 1e-5
+    assert root[3] == ot["m"][o.nn]
+    assert root[0] == ot["x"][o.nn] and root[1] == ot["y"][o.nn] and root[2] == ot["z"][o.nn]
+
+
+def test_batch_of_universes_matches_oracle_per_universe():
+    """Several uneven universes in one sim: each equals the oracle run on it alone."""
+    import nbh
+    from nbh import universe as U
+    counts = [1024, 33, 5000, 1, 12000, 2048]
+    parts = [U.PlummerUniverseGenerator(seed=40 + i).arrays(c) for i, c in enumerate(counts)]
+    cat = [np.concatenate([p[k] for p in parts]) for k in range(7)]
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    g.load_batch(counts, *cat)
+    g.step(3)
+    gs = g.read()
+    total_inter = 0
+    off = 0
+    for i, c in enumerate(counts):
+        o = oracle_for(c, theta=0.5, eps=0.05, dt=0.01, vote=32, fma=True)
+        o.load(*parts[i])
+        o.step(3)
+        os_ = o.state()
+        sl = slice(off, off + c)
+        sub = {k: gs[k][sl] for k in KEYS}
+        rel, _ = acc_rel(sub, os_)
+        assert rel.max() <= FMA_ACC_REL_MAX, (i, rel.max())
+        for k in ("x", "y", "z"):
+            assert np.abs(sub[k] - os_[k]).max() <= 1e-5 * max(1.0, np.abs(os_[k]).max())
+        total_inter += o.interactions
+        off += c
+    assert g.stats()["interactions"] == total_inter
+    assert isinstance(nbh.Simulation, type)
+
+
+def test_graph_and_eager_paths_identical():
+    n = 8192
+    arrs = plummer(n, seed=2)
+    outs = []
+    for use_graph, timing in ((True, False), (False, False), (False, True)):
+        g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, use_graph=use_graph, stage_timing=timing)
+        g.load(*arrs)
+        g.step(4)
+        outs.append(g.read())
+        if timing:
+            st = g.stats()
+            assert st["ms_force"] > 0 and st["ms_step"] >= st["ms_force"]
+    for o in outs[1:]:
+        for k in KEYS:
+            np.testing.assert_array_equal(outs[0][k], o[k])
+
+
+def test_precise_mode_matches_oracle():
+    """Kahan-compensated updates and FP64 root/extent, GPU vs oracle in the same mode."""
+    n = 8192
+    arrs = plummer(n, seed=12)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, precise=True)
+    g.load(*arrs)
+    o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=32, fma=True, precise=True)
+    o.load(*arrs)
+    g.step(5)
+    o.step(5)
+    gs, os_ = g.read(), o.state()
+    rel, _ = acc_rel(gs, os_)
+    assert rel.max() <= FMA_ACC_REL_MAX
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        assert np.abs(gs[k] - os_[k]).max() <= 1e-5 * np.abs(os_[k]).max()
+
+
+def test_direct_f64_matches_oracle():
+    import oracle as O
+    n = 30000
+    arrs = plummer(n, seed=21)
+    g = gpu_sim(theta=0.5, eps=0.05)
+    g.load(*arrs)
+    idx = np.random.default_rng(0).choice(n, 97, replace=False).astype(np.int32)
+    ga = g.direct_f64(idx)
+    oa = O.direct_f64(arrs[0], arrs[1], arrs[2], arrs[6], 0.05, idx)
+    for a, b in zip(ga, oa):
+        np.testing.assert_allclose(a, b, rtol=1e-10, atol=1e-12)
+
+
+def test_force_error_vs_fp64_plummer():
+    """theta 0.5 on a 65,536-body Plummer sphere: median and p99 relative force error
+    against the FP64 direct sum on 1,024 sampled bodies."""
+    import oracle as O
+    n = 65536
+    arrs = plummer(n, seed=33)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    g.load(*arrs)
+    g.step()
+    gs = g.read()
+    idx = np.random.default_rng(1).choice(n, 1024, replace=False).astype(np.int32)
+    # accelerations of step 1 belong to the positions before the drift
+    g2 = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    g2.load(*arrs)
+    ref = g2.direct_f64(idx)
+    err = O.rel_force_error(gs["ax"][idx], gs["ay"][idx], gs["az"][idx], *ref)
+    assert np.median(err) < 2e-3, np.median(err)
+    assert np.percentile(err, 99) < 2e-2, np.percentile(err, 99)
+
+
+def test_export_float4_matches_read():
+    import torch
+    n = 5000
+    arrs = plummer(n, seed=4)
+    g = gpu_sim()
+    g.load(*arrs)
+    g.step(2)
+    pos4 = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    vel4 = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    g.export_float4(pos4.data_ptr(), vel4.data_ptr())
+    st = g.read()
+    p, v = pos4.cpu().numpy(), vel4.cpu().numpy()
+    np.testing.assert_array_equal(p[:, 0], st["x"])
+    np.testing.assert_array_equal(v[:, 2], st["vz"])
+    assert (p[:, 3] == 1).all() and (v[:, 3] == 1).all()
+
+
+def test_write_resumes_from_checkpoint():
+    """Read the state after 3 steps, write it into a fresh sim whose step counter is
+    advanced the same way: the next steps agree bit for bit."""
+    n = 6000
+    arrs = plummer(n, seed=8)
+    a = gpu_sim(dt=0.01)
+    a.load(*arrs)
+    a.step(3)
+    ck = a.read()
+    b = gpu_sim(dt=0.01)
+    b.load(*arrs)
+    b.step(3)                          # same step counter as a
+    b.write(*[ck[k] for k in KEYS])
+    a.step(2)
+    b.step(2)
+    ra, rb = a.read(), b.read()
+    for k in KEYS:
+        np.testing.assert_array_equal(ra[k], rb[k])
