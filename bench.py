@@ -190,6 +190,8 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--error-samples", type=int, default=4096)
+    ap.add_argument("--profile-only", action="store_true",
+                    help="load, warm up and run the timed steps only (for ncu captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -217,14 +219,16 @@ def main():
     sim.load(*arrs)
 
     # force error of the first step against the FP64 direct sum on sampled bodies
-    rng = np.random.default_rng(17)
-    idx = rng.choice(n, min(args.error_samples, n), replace=False).astype(np.int32)
-    ref = sim.direct_f64(idx)
-    sim.step(1)
-    st0 = sim.read()
-    err = O.rel_force_error(st0["ax"][idx], st0["ay"][idx], st0["az"][idx], *ref)
-    force_error = {"median": float(np.median(err)), "p99": float(np.percentile(err, 99)),
-                   "samples": int(idx.size), "vs": "FP64 direct sum"}
+    force_error = None
+    if not args.profile_only:
+        rng = np.random.default_rng(17)
+        idx = rng.choice(n, min(args.error_samples, n), replace=False).astype(np.int32)
+        ref = sim.direct_f64(idx)
+        sim.step(1)
+        st0 = sim.read()
+        err = O.rel_force_error(st0["ax"][idx], st0["ay"][idx], st0["az"][idx], *ref)
+        force_error = {"median": float(np.median(err)), "p99": float(np.percentile(err, 99)),
+                       "samples": int(idx.size), "vs": "FP64 direct sum"}
 
     stream = torch.cuda.ExternalStream(sim.stream, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -266,6 +270,12 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     interactions = int(st["interactions"])
+
+    if args.profile_only:
+        if rank == 0:
+            print(json.dumps({"profile_only": True, "ms_per_step": ms, "interactions": interactions}))
+        sim.close()
+        return 0
 
     # per-stage device times (eager launches with events between stages)
     hbm_peak, peak_src = _peaks()

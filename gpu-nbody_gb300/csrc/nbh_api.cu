@@ -28,7 +28,9 @@ struct nbh_sim {
     int cap_body = 0, cap_nodes = 0, cap_univ = 0, cap_chunks = 0, cap_warps = 0;
     // device buffers
     float4 *node4 = nullptr, *vel = nullptr, *acc = nullptr, *kpos = nullptr, *kvel = nullptr;
+    float4* kids4 = nullptr;
     int *child = nullptr, *count = nullptr, *start = nullptr, *arrive = nullptr, *parent = nullptr;
+    int* loff = nullptr;
     int* sorted = nullptr;
     DevState* st = nullptr;
     int* ubody = nullptr;
@@ -92,13 +94,13 @@ int grow(nbh_sim* sim, T** ptr, size_t count, size_t* cap_unused = nullptr) {
 }
 
 void free_buffers(nbh_sim* sim) {
-    void* ptrs[] = {sim->node4, sim->vel, sim->acc, sim->kpos, sim->kvel, sim->child, sim->count,
+    void* ptrs[] = {sim->loff, sim->kids4, sim->node4, sim->vel, sim->acc, sim->kpos, sim->kvel, sim->child, sim->count,
                     sim->start, sim->arrive, sim->parent, sim->sorted, sim->ubody, sim->ubox,
                     sim->uradius, sim->chunks, sim->warps, sim->staging, sim->theta_body};
     for (void* p : ptrs)
         if (p) cudaFree(p);
-    sim->node4 = sim->vel = sim->acc = sim->kpos = sim->kvel = nullptr;
-    sim->child = sim->count = sim->start = sim->arrive = sim->parent = sim->sorted = nullptr;
+    sim->kids4 = sim->node4 = sim->vel = sim->acc = sim->kpos = sim->kvel = nullptr;
+    sim->child = sim->count = sim->start = sim->arrive = sim->parent = sim->sorted = sim->loff = nullptr;
     sim->ubody = nullptr;
     sim->ubox = nullptr;
     sim->uradius = nullptr;
@@ -122,7 +124,9 @@ StepParams params(const nbh_sim* sim) {
     p.kpos = sim->kpos;
     p.kvel = sim->kvel;
     p.child = sim->child;
+    p.kids4 = sim->kids4;
     p.count = sim->count;
+    p.loff = sim->loff;
     p.start = sim->start;
     p.arrive = sim->arrive;
     p.parent = sim->parent;
@@ -157,6 +161,7 @@ void enqueue_step(nbh_sim* sim, bool timed) {
     launch_bbox(p, sim->grid_bbox, s);
     if (timed) cudaEventRecord(sim->ev[1], s);
     launch_build(p, sim->grid_build, s);
+    launch_link(p, sim->grid_sum, s);
     if (timed) cudaEventRecord(sim->ev[2], s);
     launch_summarize(p, ref, sim->grid_sum, s);
     if (timed) cudaEventRecord(sim->ev[3], s);
@@ -187,10 +192,10 @@ int set_geometry(nbh_sim* sim) {
     CK(static_cast<cudaError_t>(occupancy_force(sim->cfg.vote_width, sim->cfg.arith == NBH_ARITH_REFERENCE,
                                                 &occ_force)));
     sim->grid_bbox = std::max(1, std::min(sim->nchunks, 4 * sms));
-    sim->grid_build = std::max(1, std::min(sim->nchunks, 8 * sms));
-    sim->grid_sum = std::max(1, std::min((sim->nbody + 255) / 256, 8 * sms));
-    // The sort's waits need every block resident: one full wave, never more.
-    sim->grid_sort = std::max(1, std::min(occ_sort * sms, (sim->ncells + 255) / 256 + sms));
+    // one body per thread: a long insertion or climb never delays another body
+    sim->grid_build = std::max(1, sim->nchunks);
+    sim->grid_sum = std::max(1, (sim->nbody + 255) / 256);
+    sim->grid_sort = std::max(1, std::min(occ_sort * sms, (sim->ncells + 255) / 256));
     sim->grid_force = std::max(1, occ_force * sms);
     sim->grid_int = std::max(1, std::min((sim->nbody + 255) / 256, 4 * sms));
     return NBH_OK;
@@ -226,7 +231,9 @@ int alloc_for(nbh_sim* sim, int nbody, int nuniv, int nnodes, int nchunks, int n
     if ((e = grow(sim, &sim->kpos, (size_t)nbody))) return e;
     if ((e = grow(sim, &sim->kvel, (size_t)nbody))) return e;
     if ((e = grow(sim, &sim->child, (size_t)8 * ncells))) return e;
+    if ((e = grow(sim, &sim->kids4, (size_t)8 * ncells))) return e;
     if ((e = grow(sim, &sim->count, (size_t)ncells))) return e;
+    if ((e = grow(sim, &sim->loff, (size_t)ncells))) return e;
     if ((e = grow(sim, &sim->start, (size_t)ncells))) return e;
     if ((e = grow(sim, &sim->arrive, (size_t)ncells))) return e;
     if ((e = grow(sim, &sim->parent, (size_t)nnodes + 1))) return e;
@@ -314,6 +321,11 @@ int nbh_create(const nbh_config* cfg_in, nbh_sim** out) {
     }
     for (auto& ev : sim->ev) cudaEventCreate(&ev);
     std::memset(sim->h_state, 0, sizeof(DevState));
+    if ((e = static_cast<cudaError_t>(prepare_force_kernels())) != cudaSuccess) {
+        fail(nullptr, NBH_ERR_CUDA, std::string("nbh_create: ") + cudaGetErrorString(e));
+        nbh_destroy(sim);
+        return NBH_ERR_CUDA;
+    }
     *out = sim;
     return NBH_OK;
 }
@@ -357,7 +369,7 @@ int nbh_load_batch(nbh_sim* sim, int32_t nuniv, const int32_t* counts, const flo
     // universe tables
     sim->h_ubody.assign(nuniv + 1, 0);
     for (int u = 0; u < nuniv; ++u) sim->h_ubody[u + 1] = sim->h_ubody[u] + counts[u];
-    const int target = std::max(256, std::min(4096, (n + 8 * sim->sms - 1) / (8 * sim->sms)));
+    const int target = 256;   // bodies per chunk = threads per block of the build
     std::vector<int4> chunks;
     std::vector<int2> warps;
     for (int u = 0; u < nuniv; ++u) {

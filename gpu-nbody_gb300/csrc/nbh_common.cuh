@@ -9,10 +9,12 @@
 //
 // Per node:   float4 node4[i]   = (x, y, z, mass): body position, cell centre during the
 //                                  build, cell centre of mass after summarize
-//             int    parent[i]  = enclosing cell (-1 for roots)
+//             int    parent[i]  = enclosing cell (-1 for roots), set by the link pass
 // Per cell c (offset k = c - nbody):
 //             int    child[8k .. 8k+7]  child slots, -1 empty, -2 locked (buildtree.cl:7-8)
-//             int    count[k], start[k], arrive[k]
+//             float4 kids4[8k .. 8k+7]  copies of the children's node records, in slot
+//                                       order, written by summarize for the force walk
+//             int    count[k], start[k], loff[k], arrive[k]
 // Per body:   float4 vel[b], acc[b]  (w unused), sorted[s] = body at depth-first position s
 #pragma once
 #include <cstdint>
@@ -51,8 +53,10 @@ struct StepParams {
     float4* kpos;        // Kahan compensation of positions (precise mode), may be null
     float4* kvel;        // Kahan compensation of velocities (precise mode), may be null
     int* child;          // 8 * ncells
+    float4* kids4;       // 8 * ncells: node records of each cell's children (slot order)
     int* count;          // ncells
-    int* start;          // ncells
+    int* start;          // ncells: first depth-first position of each cell
+    int* loff;           // ncells: offset of a cell inside its parent's depth-first range
     int* arrive;         // ncells
     int* parent;         // nnodes + 1
     int* sorted;         // nbody
@@ -105,6 +109,9 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
     int v;
     asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
+}
+__device__ __forceinline__ void st_relaxed(int* p, int v) {
+    asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 __device__ __forceinline__ void st_release(int* p, int v) {
     asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");

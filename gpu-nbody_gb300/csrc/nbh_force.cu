@@ -1,49 +1,102 @@
-// nbh_force.cu — force traversal, leapfrog integration, host<->device packing and the
-// FP64 direct sum used to measure force error.
+// nbh_force.cu — the force stage: Barnes-Hut tree walk with a group-voted opening test.
 #include "nbh_common.cuh"
 #include "nbh_kernels.h"
 
 namespace nbh {
 
-constexpr int kForceThreads = 256;
-constexpr int kForceWarps = kForceThreads / 32;
+constexpr int kForceThreads = 128;
+// Per-group stack of pending children, each with its preloaded node record.  Opening a
+// cell at level l while every ancestor still has 7 pending children needs 7*l + 8
+// entries, so kStackCap entries cover trees up to kFastMaxDepth levels; deeper trees (or
+// pools beyond kFastMaxNodes) take the per-level (cell, next child) walk.
+constexpr int kStackCap = 256;
+constexpr int kFastMaxDepth = (kStackCap - 8) / 7 + 1;
+
+template <int W>
+constexpr size_t force_smem_bytes() {
+    return (size_t)(kForceThreads / W) * kStackCap * (sizeof(float4) + sizeof(int2));
+}
 
 // Opening threshold of tree level L (root = 0): r^2/theta^2 * 4^-L + eps^2
-// (calculateforce.cl:52-67; the reference's repeated *0.25 equals ldexp in the normal
-// range and eps^2 absorbs the term below it).
+// (calculateforce.cl:52-67).  The walk carries s = 4^-L (exact powers of two) and forms
+// t0*s + eps^2, which equals ldexp(t0, -2L) + eps^2 in the normal range; below it eps^2
+// absorbs the term either way.
 __device__ __forceinline__ float level_dq(float t0, int level, float eps2) {
     return __fadd_rn(ldexpf(t0, -2 * level), eps2);
+}
+
+// 1/sqrt(d2).  d2 >= eps^2 > 0 is never subnormal, so the flush-to-zero form of the
+// hardware approximation returns exactly what rsqrtf would.
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+template <bool REF>
+__device__ __forceinline__ void interact(const float4 q, const float dx, const float dy, const float dz,
+                                         const float d2, float& ax, float& ay, float& az) {
+    float rd;
+    if constexpr (REF) rd = __fdiv_rn(1.0f, __fsqrt_rn(d2));
+    else rd = rsqrt_ftz(d2);
+    const float f = __fmul_rn(__fmul_rn(__fmul_rn(q.w, rd), rd), rd);
+    ax = madd<REF>(dx, f, ax);
+    ay = madd<REF>(dy, f, ay);
+    az = madd<REF>(dz, f, az);
+}
+
+template <bool REF>
+__device__ __forceinline__ float dist2(const float dx, const float dy, const float dz, const float eps2) {
+    if constexpr (REF)
+        return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)), eps2);
+    else
+        return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmaf_rn(dz, dz, eps2)));
 }
 
 // -------------------------------------------------------------------------------------
 // Force (calculateforce.cl:52-185).  A group of W lanes (W = 32: one warp; W = 16: the
 // reference's work-group, :99,145) takes W consecutive bodies of the depth-first order and
-// walks its universe's tree with one shared stack of (cell, next child) per level.  A body
-// child is always accepted; a cell child only if every body of the group sees
-// d^2 + eps^2 >= dq[level] (work_group_all, :145), else it is opened.  Children are
-// compacted, so the first empty slot ends a cell.  The walk is depth-first in child order,
-// so every body accumulates its interactions in the reference's order.  Work items (32
-// bodies) are handed out dynamically for balance.  After the walk: the leapfrog velocity
-// correction for step > 0 (:174-181) and the acceleration store (:183-185).
+// walks its universe's tree.  A body child is always accepted; a cell child only if every
+// body of the group sees d^2 + eps^2 >= dq[level] (work_group_all, :145), else it is
+// opened.  The walk is depth-first in child order (children are compacted, so the first
+// empty slot ends a cell), so every body accumulates its interactions in the reference's
+// order.  Every lane of a group accepts the same children, so the group's interaction
+// count is counted once per opened cell, not per visit.
+//
+// GB300 schedule: opening a cell loads its 8 child slots and the 8 node records that
+// summarize stored next to them (kids4) with one load per lane -- one round trip per
+// opened cell -- and pushes them, first child on top, onto the group's shared-memory
+// stack with their level factor 4^-level (-1 for bodies, which makes the test pass);
+// each visit reads one record from shared memory and needs no branch on its kind.  Lanes
+// past the end of a universe walk with their group's first body, so they never change a
+// vote and need no predicate.  Work items (32 bodies) are handed out dynamically.
+// After the walk: the leapfrog velocity correction for step > 0 (:174-181) and the
+// acceleration store (:183-185).
 //
 // REF: reference arithmetic (rounded products, 1/sqrt correctly rounded); otherwise FMA and
 // the hardware inverse square root.  PB: per-body opening angle from theta_body.
 template <int W, bool REF, bool PB>
 __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
     if (load_status(p.st)) return;
-    constexpr int kGroups = kForceWarps * (32 / W);
-    __shared__ int s_node[kGroups][kMaxDepth];
-    __shared__ int s_next[kGroups][kMaxDepth];
+    constexpr int kGroups = kForceThreads / W;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4* const sq_all = reinterpret_cast<float4*>(smem_raw);
+    int2* const se_all = reinterpret_cast<int2*>(sq_all + kGroups * kStackCap);
     const int lane = threadIdx.x & 31;
-    const int grp = (threadIdx.x >> 5) * (32 / W) + lane / W;
+    const int grp = threadIdx.x / W;
+    const int glane = threadIdx.x % W;
     const unsigned gmask = (W == 32) ? 0xffffffffu : (0xffffu << (16 * (lane >> 4)));
-    int* const snode = s_node[grp];
-    int* const snext = s_next[grp];
+    float4* const sq = sq_all + grp * kStackCap;     // node record of each pending child
+    int2* const se = se_all + grp * kStackCap;       // (node index, bits of 4^-level or -1)
+    int* const snode = reinterpret_cast<int*>(se);   // deep-tree walk: (cell, next) per level
+    int* const snext = snode + kMaxDepth;
     const int nbody = p.nbody;
     const float eps2 = p.eps2;
     const int step = p.st->step;
+    const bool fast = p.st->max_depth <= kFastMaxDepth;
     const float4* __restrict__ node4 = p.node4;
     const int* __restrict__ child = p.child;
+    const float4* __restrict__ kids4 = p.kids4;
     unsigned long long my_inter = 0;
 
     for (;;) {
@@ -55,76 +108,116 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
         const int u = wi.y;
         const int s = wi.x + lane;
         const bool valid = s < p.ubody[u + 1];
-        int b = 0;
-        float4 pb = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (valid) {
-            b = p.sorted[s];
-            pb = node4[b];
-        }
+        // Lanes past the universe's end take their group's first body.
+        const int sg = valid ? s : wi.x + (lane / W) * W;
+        const bool gvalid = sg < p.ubody[u + 1];       // the group has any body at all
+        const int b = gvalid ? p.sorted[sg] : 0;
+        const float4 pb = node4[b];
         const float r = p.uradius[u];
         const float rr = __fmul_rn(r, r);
         float th2 = p.theta2;
         if constexpr (PB) {
-            if (valid) {
-                const float th = p.theta_body[b];
-                th2 = __fmul_rn(th, th);
-            }
+            const float th = p.theta_body[b];
+            th2 = __fmul_rn(th, th);
         }
         const float t0 = th2 > 0.0f ? __fdiv_rn(rr, th2) : rr;
         float ax = 0.f, ay = 0.f, az = 0.f;
-        int ninter = 0;
+        long long ninter = 0;
+        const int root = p.nnodes - u;
 
-        if (__any_sync(gmask, valid)) {
-            int depth = 0;
-            int node = p.nnodes - u;
-            int k = 0;
-            float dq = level_dq(t0, 0, eps2);
-            for (;;) {
-                int ch = kNull;
-                if (k < 8) ch = __ldg(child + ((size_t)(node - nbody) << 3) + k);
-                if (ch < 0) {
-                    // end of this cell (:165-171): back to the parent's next child
-                    if (depth == 0) break;
-                    --depth;
-                    node = snode[depth];
-                    k = snext[depth];
-                    dq = level_dq(t0, depth, eps2);
-                    continue;
+        if (gvalid) {
+            if (fast) {
+                int top = 0;
+                int pushed = 0, opened = -1;
+                int open = root;
+                float open_s = 1.0f;                      // 4^-level of open's children
+                bool ok = true;
+                for (;;) {
+                    if (open >= 0) {
+                        // push the children of `open`, first child on top
+                        int chk = kNull;
+                        float4 qk = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (glane < 8) {
+                            const size_t o8 = ((size_t)(open - nbody) << 3) + glane;
+                            chk = __ldg(child + o8);
+                            qk = __ldg(kids4 + o8);
+                        }
+                        const unsigned bal = __ballot_sync(gmask, glane < 8 && chk >= 0) & gmask;
+                        const int cnt = __popc(bal);
+                        if (top + cnt > kStackCap) {           // unreachable below kFastMaxDepth
+                            raise_error(p.st, NBH_ERR_DEPTH);
+                            ok = false;
+                            break;
+                        }
+                        if (glane < cnt) {
+                            const int slot = top + cnt - 1 - glane;
+                            sq[slot] = qk;
+                            se[slot] = make_int2(chk, __float_as_int(chk >= nbody ? open_s : -1.0f));
+                        }
+                        top += cnt;
+                        pushed += cnt;
+                        ++opened;
+                        open = -1;
+                        __syncwarp(gmask);
+                    }
+                    if (top == 0) break;
+                    --top;
+                    const int2 e = se[top];
+                    const float4 q = sq[top];
+                    const float dx = __fsub_rn(q.x, pb.x);
+                    const float dy = __fsub_rn(q.y, pb.y);
+                    const float dz = __fsub_rn(q.z, pb.z);
+                    const float d2 = dist2<REF>(dx, dy, dz, eps2);
+                    const float sl = __int_as_float(e.y);
+                    const float dq = __fadd_rn(__fmul_rn(t0, sl), eps2);
+                    if (__all_sync(gmask, d2 >= dq)) {
+                        interact<REF>(q, dx, dy, dz, d2, ax, ay, az);
+                    } else {
+                        open = e.x;
+                        open_s = __fmul_rn(sl, 0.25f);
+                        __syncwarp(gmask);     // every lane has read the stack before it is refilled
+                    }
                 }
-                ++k;
-                const float4 q = __ldg(node4 + ch);
-                const float dx = __fsub_rn(q.x, pb.x);
-                const float dy = __fsub_rn(q.y, pb.y);
-                const float dz = __fsub_rn(q.z, pb.z);
-                float d2;
-                if constexpr (REF)
-                    d2 = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)), eps2);
-                else
-                    d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmaf_rn(dz, dz, eps2)));
-                const bool accept = ch < nbody || __all_sync(gmask, !valid || d2 >= dq);
-                if (accept) {
-                    if (valid) {
-                        float rd;
-                        if constexpr (REF) rd = __fdiv_rn(1.0f, __fsqrt_rn(d2));
-                        else rd = rsqrtf(d2);
-                        const float f = __fmul_rn(__fmul_rn(__fmul_rn(q.w, rd), rd), rd);
-                        ax = madd<REF>(dx, f, ax);
-                        ay = madd<REF>(dy, f, ay);
-                        az = madd<REF>(dz, f, az);
+                if (ok) ninter = pushed - opened;
+            } else {
+                // Deep trees: per-level (cell, next child) walk (calculateforce.cl:112-172).
+                int depth = 0;
+                int node = root;
+                int k = 0;
+                float dq = level_dq(t0, 0, eps2);
+                for (;;) {
+                    int ch = kNull;
+                    if (k < 8) ch = __ldg(child + ((size_t)(node - nbody) << 3) + k);
+                    if (ch < 0) {
+                        if (depth == 0) break;
+                        --depth;
+                        node = snode[depth];
+                        k = snext[depth];
+                        dq = level_dq(t0, depth, eps2);
+                        continue;
+                    }
+                    ++k;
+                    const float4 q = __ldg(node4 + ch);
+                    const float dx = __fsub_rn(q.x, pb.x);
+                    const float dy = __fsub_rn(q.y, pb.y);
+                    const float dz = __fsub_rn(q.z, pb.z);
+                    const float d2 = dist2<REF>(dx, dy, dz, eps2);
+                    if (ch < nbody || __all_sync(gmask, d2 >= dq)) {
+                        interact<REF>(q, dx, dy, dz, d2, ax, ay, az);
                         ++ninter;
+                    } else {
+                        if (depth + 1 >= kMaxDepth) {   // unreachable for a tree the build accepted
+                            raise_error(p.st, NBH_ERR_DEPTH);
+                            break;
+                        }
+                        // every lane writes the same entry, so no lane reads a stale one
+                        snode[depth] = node;
+                        snext[depth] = k;
+                        ++depth;
+                        node = ch;
+                        k = 0;
+                        dq = level_dq(t0, depth, eps2);
                     }
-                } else {
-                    // open the cell (:155-163); every lane writes the same stack entry
-                    if (depth + 1 >= kMaxDepth) {   // unreachable for a tree the build accepted
-                        raise_error(p.st, NBH_ERR_DEPTH);
-                        break;
-                    }
-                    snode[depth] = node;
-                    snext[depth] = k;
-                    ++depth;
-                    node = ch;
-                    k = 0;
-                    dq = level_dq(t0, depth, eps2);
                 }
             }
         }
@@ -158,6 +251,7 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
             p.acc[b] = make_float4(ax, ay, az, 0.0f);
             my_inter += (unsigned long long)ninter;
         }
+        __syncwarp();
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) my_inter += __shfl_xor_sync(0xffffffffu, my_inter, o);
@@ -165,180 +259,30 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
 }
 
 // -------------------------------------------------------------------------------------
-// Integrate (integrate.cl:27-43): dv = a*dt*0.5; v' = v + dv; x += v'*dt; v = v' + dv.
-// Precise mode: the drift v'*dt and the kick a*dt are Kahan-compensated sums.
-template <bool REF, bool PRECISE>
-__global__ void __launch_bounds__(256) integrate_kernel(StepParams p) {
-    if (load_status(p.st)) return;
-    const float dt = p.dt;
-    const int stride = gridDim.x * blockDim.x;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.nbody; i += stride) {
-        float4 x = p.node4[i];
-        float4 v = p.vel[i];
-        const float4 a = p.acc[i];
-        const float dvx = __fmul_rn(__fmul_rn(a.x, dt), 0.5f);
-        const float dvy = __fmul_rn(__fmul_rn(a.y, dt), 0.5f);
-        const float dvz = __fmul_rn(__fmul_rn(a.z, dt), 0.5f);
-        const float hx = __fadd_rn(v.x, dvx), hy = __fadd_rn(v.y, dvy), hz = __fadd_rn(v.z, dvz);
-        if constexpr (PRECISE) {
-            float4 kx = p.kpos[i], kv = p.kvel[i];
-            float y1, t1;
-            y1 = __fsub_rn(__fmul_rn(hx, dt), kx.x); t1 = __fadd_rn(x.x, y1); kx.x = __fsub_rn(__fsub_rn(t1, x.x), y1); x.x = t1;
-            y1 = __fsub_rn(__fmul_rn(hy, dt), kx.y); t1 = __fadd_rn(x.y, y1); kx.y = __fsub_rn(__fsub_rn(t1, x.y), y1); x.y = t1;
-            y1 = __fsub_rn(__fmul_rn(hz, dt), kx.z); t1 = __fadd_rn(x.z, y1); kx.z = __fsub_rn(__fsub_rn(t1, x.z), y1); x.z = t1;
-            y1 = __fsub_rn(__fmul_rn(a.x, dt), kv.x); t1 = __fadd_rn(v.x, y1); kv.x = __fsub_rn(__fsub_rn(t1, v.x), y1); v.x = t1;
-            y1 = __fsub_rn(__fmul_rn(a.y, dt), kv.y); t1 = __fadd_rn(v.y, y1); kv.y = __fsub_rn(__fsub_rn(t1, v.y), y1); v.y = t1;
-            y1 = __fsub_rn(__fmul_rn(a.z, dt), kv.z); t1 = __fadd_rn(v.z, y1); kv.z = __fsub_rn(__fsub_rn(t1, v.z), y1); v.z = t1;
-            p.kpos[i] = kx;
-            p.kvel[i] = kv;
-        } else {
-            x.x = madd<REF>(hx, dt, x.x);
-            x.y = madd<REF>(hy, dt, x.y);
-            x.z = madd<REF>(hz, dt, x.z);
-            v.x = __fadd_rn(hx, dvx);
-            v.y = __fadd_rn(hy, dvy);
-            v.z = __fadd_rn(hz, dvz);
-        }
-        p.node4[i] = x;
-        p.vel[i] = v;
-    }
-}
-
-// -------------------------------------------------------------------------------------
-// SoA <-> float4 packing for nbh_load / nbh_write / nbh_read and the float4 export of
-// copyvertices.cl:14-17.  mask bits: 1 pos, 2 vel, 4 acc, 8 mass.
-__global__ void pack_kernel(int n, const float* __restrict__ soa, int mask, float4* node4,
-                            float4* vel, float4* acc) {
-    const int stride = gridDim.x * blockDim.x;
-    const float* X = soa;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        if (mask & 9) {
-            float4 q = node4[i];
-            if (mask & 1) { q.x = X[i]; q.y = X[n + i]; q.z = X[2 * n + i]; }
-            if (mask & 8) q.w = X[9 * n + i];
-            node4[i] = q;
-        }
-        if (mask & 2) vel[i] = make_float4(X[3 * n + i], X[4 * n + i], X[5 * n + i], 0.f);
-        if (mask & 4) acc[i] = make_float4(X[6 * n + i], X[7 * n + i], X[8 * n + i], 0.f);
-    }
-}
-
-__global__ void unpack_kernel(int n, float* __restrict__ soa, const float4* node4, const float4* vel,
-                              const float4* acc) {
-    const int stride = gridDim.x * blockDim.x;
-    float* X = soa;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float4 q = node4[i], v = vel[i], a = acc[i];
-        X[i] = q.x; X[n + i] = q.y; X[2 * n + i] = q.z;
-        X[3 * n + i] = v.x; X[4 * n + i] = v.y; X[5 * n + i] = v.z;
-        X[6 * n + i] = a.x; X[7 * n + i] = a.y; X[8 * n + i] = a.z;
-    }
-}
-
-__global__ void export4_kernel(int n, const float4* node4, const float4* vel, float4* pos4, float4* vel4) {
-    const int stride = gridDim.x * blockDim.x;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        if (pos4) { float4 q = node4[i]; q.w = 1.0f; pos4[i] = q; }
-        if (vel4) { float4 v = vel[i]; v.w = 1.0f; vel4[i] = v; }
-    }
-}
-
-// -------------------------------------------------------------------------------------
-// FP64 direct sum a_i = G sum_j m_j (x_j - x_i) / (|x_j - x_i|^2 + eps^2)^(3/2) for a list
-// of bodies, each over the bodies [lo, hi) of its own universe.  Sources are split across
-// blockIdx.y and the partial sums added atomically (outputs zeroed by the caller).
-constexpr int kDirectTile = 256;
-struct Src64 {
-    double x, y, z, m;
-};
-__global__ void __launch_bounds__(kDirectTile) direct_f64_kernel(const float4* __restrict__ node4, int nidx,
-                                                                 const int* __restrict__ idx,
-                                                                 const int2* __restrict__ range, double eps2,
-                                                                 double G, double* out) {
-    __shared__ Src64 tile[kDirectTile];
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = t < nidx;
-    int i = 0;
-    int2 rg = make_int2(0, 0);
-    if (valid) {
-        i = idx[t];
-        rg = range[t];
-    }
-    // the block's source range: union of its targets' universes
-    __shared__ int blo, bhi;
-    if (threadIdx.x == 0) { blo = 0x7fffffff; bhi = 0; }
-    __syncthreads();
-    if (valid) { atomicMin(&blo, rg.x); atomicMax(&bhi, rg.y); }
-    __syncthreads();
-    const int lo = blo, hi = bhi;
-    if (lo >= hi) return;
-    const int len = hi - lo;
-    const int per = (len + gridDim.y - 1) / gridDim.y;
-    const int s0 = lo + blockIdx.y * per;
-    const int s1 = min(hi, s0 + per);
-    double xi = 0, yi = 0, zi = 0;
-    if (valid) {
-        const float4 q = node4[i];
-        xi = q.x; yi = q.y; zi = q.z;
-    }
-    double sx = 0, sy = 0, sz = 0;
-    for (int base = s0; base < s1; base += kDirectTile) {
-        const int j = base + threadIdx.x;
-        __syncthreads();
-        if (j < s1) {
-            const float4 q = node4[j];
-            tile[threadIdx.x] = Src64{q.x, q.y, q.z, q.w};
-        }
-        __syncthreads();
-        const int cnt = min(kDirectTile, s1 - base);
-        if (valid) {
-            for (int k = 0; k < cnt; ++k) {
-                const int jj = base + k;
-                if (jj < rg.x || jj >= rg.y) continue;
-                const Src64 q = tile[k];
-                const double dx = q.x - xi, dy = q.y - yi, dz = q.z - zi;
-                const double d2 = dx * dx + dy * dy + dz * dz + eps2;
-                const double inv = 1.0 / sqrt(d2);
-                const double f = q.m * inv * inv * inv;
-                sx += dx * f;
-                sy += dy * f;
-                sz += dz * f;
-            }
-        }
-    }
-    if (valid) {
-        atomicAdd(out + 3 * t + 0, G * sx);
-        atomicAdd(out + 3 * t + 1, G * sy);
-        atomicAdd(out + 3 * t + 2, G * sz);
-    }
-}
-
-// -------------------------------------------------------------------------------------
-// FP32 FMA throughput probe: 8 independent dependency chains per thread keep the FMA
-// pipes busy; the result is stored so nothing is optimised away.
-__global__ void __launch_bounds__(256) fma_peak_kernel(float* sink, int iters) {
-    float a[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) a[k] = (float)(threadIdx.x + k) * 1e-3f;
-    const float b = 0.999f, c = 1e-4f;
-    for (int i = 0; i < iters; ++i) {
-#pragma unroll
-        for (int k = 0; k < 8; ++k) a[k] = __fmaf_rn(a[k], b, c);
-    }
-    float s = 0.f;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) s += a[k];
-    sink[(blockIdx.x * blockDim.x + threadIdx.x) & (1024 * 1024 - 1)] = s;
-}
-
-void launch_fma_peak(float* sink, int iters, int grid, int block, cudaStream_t s) {
-    fma_peak_kernel<<<grid, block, 0, s>>>(sink, iters);
-}
-
 template <int W, bool REF>
 static void launch_force_t(const StepParams& p, bool pb, int grid, cudaStream_t s) {
-    if (pb) force_kernel<W, REF, true><<<grid, kForceThreads, 0, s>>>(p);
-    else force_kernel<W, REF, false><<<grid, kForceThreads, 0, s>>>(p);
+    constexpr size_t sm = force_smem_bytes<W>();
+    if (pb) force_kernel<W, REF, true><<<grid, kForceThreads, sm, s>>>(p);
+    else force_kernel<W, REF, false><<<grid, kForceThreads, sm, s>>>(p);
+}
+
+template <int W, bool REF, bool PB>
+static cudaError_t prep_force() {
+    return cudaFuncSetAttribute(force_kernel<W, REF, PB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)force_smem_bytes<W>());
+}
+
+int prepare_force_kernels() {
+    cudaError_t e = cudaSuccess, t;
+    if ((t = prep_force<32, false, false>()) != cudaSuccess) e = t;
+    if ((t = prep_force<32, false, true>()) != cudaSuccess) e = t;
+    if ((t = prep_force<32, true, false>()) != cudaSuccess) e = t;
+    if ((t = prep_force<32, true, true>()) != cudaSuccess) e = t;
+    if ((t = prep_force<16, false, false>()) != cudaSuccess) e = t;
+    if ((t = prep_force<16, false, true>()) != cudaSuccess) e = t;
+    if ((t = prep_force<16, true, false>()) != cudaSuccess) e = t;
+    if ((t = prep_force<16, true, true>()) != cudaSuccess) e = t;
+    return (int)e;
 }
 
 void launch_force(const StepParams& p, int vote, bool ref, int grid, cudaStream_t s) {
@@ -353,39 +297,12 @@ void launch_force(const StepParams& p, int vote, bool ref, int grid, cudaStream_
 }
 
 int occupancy_force(int vote, bool ref, int* blocks_per_sm) {
+    const size_t s16 = force_smem_bytes<16>(), s32 = force_smem_bytes<32>();
     if (vote == 16)
-        return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, true, false>, kForceThreads, 0)
-                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, false, false>, kForceThreads, 0);
-    return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<32, true, false>, kForceThreads, 0)
-               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<32, false, false>, kForceThreads, 0);
-}
-
-void launch_integrate(const StepParams& p, bool ref, int grid, cudaStream_t s) {
-    if (ref) {
-        if (p.precise) integrate_kernel<true, true><<<grid, 256, 0, s>>>(p);
-        else integrate_kernel<true, false><<<grid, 256, 0, s>>>(p);
-    } else {
-        if (p.precise) integrate_kernel<false, true><<<grid, 256, 0, s>>>(p);
-        else integrate_kernel<false, false><<<grid, 256, 0, s>>>(p);
-    }
-}
-
-void launch_pack(int n, const float* soa, int mask, float4* node4, float4* vel, float4* acc, int grid,
-                 cudaStream_t s) {
-    pack_kernel<<<grid, 256, 0, s>>>(n, soa, mask, node4, vel, acc);
-}
-void launch_unpack(int n, float* soa, const float4* node4, const float4* vel, const float4* acc, int grid,
-                   cudaStream_t s) {
-    unpack_kernel<<<grid, 256, 0, s>>>(n, soa, node4, vel, acc);
-}
-void launch_export4(int n, const float4* node4, const float4* vel, float4* pos4, float4* vel4, int grid,
-                    cudaStream_t s) {
-    export4_kernel<<<grid, 256, 0, s>>>(n, node4, vel, pos4, vel4);
-}
-void launch_direct_f64(const float4* node4, int nidx, const int* idx, const int2* range, double eps2, double G,
-                       double* out, int ysplit, cudaStream_t s) {
-    dim3 grid((nidx + kDirectTile - 1) / kDirectTile, ysplit);
-    direct_f64_kernel<<<grid, kDirectTile, 0, s>>>(node4, nidx, idx, range, eps2, G, out);
+        return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, true, false>, kForceThreads, s16)
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, false, false>, kForceThreads, s16);
+    return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<32, true, false>, kForceThreads, s32)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<32, false, false>, kForceThreads, s32);
 }
 
 }  // namespace nbh

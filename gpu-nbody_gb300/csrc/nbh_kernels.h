@@ -8,6 +8,7 @@ struct StepParams;
 
 void launch_bbox(const StepParams& p, int grid, cudaStream_t s);
 void launch_build(const StepParams& p, int grid, cudaStream_t s);
+void launch_link(const StepParams& p, int grid, cudaStream_t s);
 void launch_summarize(const StepParams& p, bool ref, int grid, cudaStream_t s);
 void launch_sort(const StepParams& p, int grid, cudaStream_t s);
 void launch_force(const StepParams& p, int vote, bool ref, int grid, cudaStream_t s);
@@ -26,5 +27,6 @@ void launch_fma_peak(float* sink, int iters, int grid, int block, cudaStream_t s
 
 int occupancy_sort(int* blocks_per_sm);
 int occupancy_force(int vote, bool ref, int* blocks_per_sm);
+int prepare_force_kernels();   // raises the dynamic shared-memory limit of the force kernels
 
 }  // namespace nbh

@@ -26,13 +26,17 @@ __global__ void __launch_bounds__(256) bbox_kernel(StepParams p) {
     __shared__ float red[6][8];
     __shared__ int last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int ci = blockIdx.x; ci < p.nchunks; ci += gridDim.x) {
-        const int4 ck = p.chunks[ci];
+    for (int ci = blockIdx.x; ci < p.nchunks;) {
+        // fold this block's consecutive chunks of one universe, then publish once
+        const int u = p.chunks[ci].x;
         float v[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
-        for (int i = ck.y + threadIdx.x; i < ck.z; i += blockDim.x) {
-            const float4 q = p.node4[i];
-            v[0] = fminf(v[0], q.x); v[1] = fminf(v[1], q.y); v[2] = fminf(v[2], q.z);
-            v[3] = fmaxf(v[3], q.x); v[4] = fmaxf(v[4], q.y); v[5] = fmaxf(v[5], q.z);
+        for (; ci < p.nchunks && p.chunks[ci].x == u; ci += gridDim.x) {
+            const int4 ck = p.chunks[ci];
+            for (int i = ck.y + threadIdx.x; i < ck.z; i += blockDim.x) {
+                const float4 q = p.node4[i];
+                v[0] = fminf(v[0], q.x); v[1] = fminf(v[1], q.y); v[2] = fminf(v[2], q.z);
+                v[3] = fmaxf(v[3], q.x); v[4] = fmaxf(v[4], q.y); v[5] = fmaxf(v[5], q.z);
+            }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -51,7 +55,7 @@ __global__ void __launch_bounds__(256) bbox_kernel(StepParams p) {
             float a = red[k][0];
             for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
                 a = k < 3 ? fminf(a, red[k][w]) : fmaxf(a, red[k][w]);
-            unsigned* box = p.ubox + 6 * ck.x;
+            unsigned* box = p.ubox + 6 * u;
             if (k < 3) atomicMin(box + k, f2ord(a));
             else atomicMax(box + k, f2ord(a));
         }
@@ -121,15 +125,9 @@ __global__ void __launch_bounds__(256) bbox_kernel(StepParams p) {
 // (:148-152) until the two bodies separate (:106-165).  The new subtree is published with
 // one release store into the locked slot (:173-180), which orders every write made under
 // the lock.  Failed locks retry from the same node (the tree only grows) with a bounded,
-// backed-off wait.  parent[] is recorded for the bottom-up summarize.
+// backed-off wait.
 __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
-    __shared__ int sdepth[8];
-    __shared__ int s_stop;
-    // This stage raises errors itself, so the entry check is made once per block: every
-    // thread of a block either runs to the final barrier or none does.
-    if (threadIdx.x == 0) s_stop = load_status(p.st);
-    __syncthreads();
-    if (s_stop) return;
+    if (load_status(p.st)) return;
     int local_max = 1;
     const int nbody = p.nbody;
     for (int ci = blockIdx.x; ci < p.nchunks; ci += gridDim.x) {
@@ -154,17 +152,21 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
                     }
                     node = ch;
                     ++depth;
-                    r *= 0.5f;
-                    const float4 c4 = ld_cg4(p.node4 + node);
-                    cx = c4.x; cy = c4.y; cz = c4.z;
+                    // The child's centre is the one its creator computed (:124-136) from this
+                    // centre and half-width, so it is derived here instead of loaded.
+                    const float h = r * 0.5f;
+                    cx = __fadd_rn(__fsub_rn(cx, h), (path & 1) ? r : 0.0f);
+                    cy = __fadd_rn(__fsub_rn(cy, h), (path & 2) ? r : 0.0f);
+                    cz = __fadd_rn(__fsub_rn(cz, h), (path & 4) ? r : 0.0f);
+                    r = h;
                     path = octant(cx, cy, cz, bp.x, bp.y, bp.z);
                     slot = cell_child(p, node) + path;
                     ch = ld_relaxed(slot);
                 }
-                if (ch != kLock && cas_acquire(slot, ch, kLock) == ch) {
+                if (ch != kLock && atomicCAS(slot, ch, kLock) == ch) {
                     if (ch == kNull) {
-                        p.parent[b] = node;
-                        st_release(slot, b);
+                        // nothing but the index itself is published: no fence needed
+                        st_relaxed(slot, b);
                     } else {
                         const int old = ch;
                         const float4 op = p.node4[old];
@@ -187,24 +189,21 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
                             cx = __fadd_rn(__fsub_rn(cx, r), ox);
                             cy = __fadd_rn(__fsub_rn(cy, r), oy);
                             cz = __fadd_rn(__fsub_rn(cz, r), oz);
-                            p.node4[cell] = make_float4(cx, cy, cz, 0.0f);
                             int* cc = cell_child(p, cell);
                             reinterpret_cast<int4*>(cc)[0] = make_int4(kNull, kNull, kNull, kNull);
                             reinterpret_cast<int4*>(cc)[1] = make_int4(kNull, kNull, kNull, kNull);
-                            p.parent[cell] = cur;
                             p.arrive[cell - nbody] = 0;
                             p.start[cell - nbody] = -1;
                             if (patch < 0) patch = cell;
                             else cell_child(p, cur)[cpath] = cell;
                             const int opath = octant(cx, cy, cz, op.x, op.y, op.z);
                             cc[opath] = old;
-                            p.parent[old] = cell;
                             cur = cell;
                             cpath = octant(cx, cy, cz, bp.x, bp.y, bp.z);
                             if (cpath != opath) break;
                         }
                         cell_child(p, cur)[cpath] = b;
-                        p.parent[b] = cur;
+                        // the new cells' centres and slots become visible before their index
                         st_release(slot, patch);
                     }
                     local_max = max(local_max, depth);
@@ -222,16 +221,27 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
         }
     }
 finish:
-    // Every thread reaches the block reduction, including those that stopped on an error.
-    __syncwarp();
+    // :199; the maximum persists across steps, so the atomic is rarely needed
+    if (local_max > ld_relaxed(&p.st->max_depth)) atomicMax(&p.st->max_depth, local_max);
+}
+
+// -------------------------------------------------------------------------------------
+// Link: parent[] of every node from the finished tree (one pass over the cells), for the
+// bottom-up summarize.  Keeping it out of the build means an insertion publishes nothing
+// but a slot value.
+__global__ void __launch_bounds__(256) link_kernel(StepParams p) {
+    if (load_status(p.st)) return;
+    const int nbody = p.nbody;
+    const int bottom = p.st->bottom;
+    const int stride = gridDim.x * blockDim.x;
+    for (int c = bottom + (int)(blockIdx.x * blockDim.x + threadIdx.x); c <= p.nnodes; c += stride) {
+        const int* ch8 = cell_child(p, c);
+        const int4 s0 = reinterpret_cast<const int4*>(ch8)[0];
+        const int4 s1 = reinterpret_cast<const int4*>(ch8)[1];
+        const int sl[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) local_max = max(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
-    if ((threadIdx.x & 31) == 0) sdepth[threadIdx.x >> 5] = local_max;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int m = sdepth[0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = max(m, sdepth[w]);
-        atomicMax(&p.st->max_depth, m);   // :199
+        for (int j = 0; j < 8; ++j)
+            if (sl[j] >= 0) p.parent[sl[j]] = c;
     }
 }
 
@@ -242,7 +252,27 @@ finish:
 // position summed in that order, centre = sum * (1/mass) (:161-167), body count
 // (:98-118,160); then it arrives at the cell's parent.  The order of the sums is fixed by
 // the octant order, independent of timing (the reference's depends on which children
-// were ready).  Precise mode sums the roots' centres of mass in FP64.
+// were ready).  Precise mode sums the roots' centres of mass in FP64.  The last arriver
+// also stores, from the registers it already holds:
+//   * the children's records as the cell's kids4 block, so the force walk reads a cell's
+//     children with one contiguous load;
+//   * each child cell's offset inside the cell's depth-first range (loff), from which the
+//     sort stage derives every start without waiting (sort.cl:44-58 hands these offsets
+//     down from the root instead).
+// Arrivals after a write are release atomics and the last arriver acquires, in place of
+// full fences.
+__device__ __forceinline__ int arrive_relaxed(int* p) {
+    int old;
+    asm volatile("atom.relaxed.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+__device__ __forceinline__ int arrive_acq_rel(int* p) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+__device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
 template <bool REF, bool PRECISE>
 __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
     if (load_status(p.st)) return;
@@ -251,6 +281,7 @@ __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
     const int stride = gridDim.x * blockDim.x;
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbody; b += stride) {
         int c = p.parent[b];
+        bool from_body = true;
         while (c >= 0) {
             int* ch8 = cell_child(p, c);
             const int4 s0 = reinterpret_cast<const int4*>(ch8)[0];
@@ -259,9 +290,15 @@ __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
             int k = 0;
 #pragma unroll
             for (int j = 0; j < 8; ++j) k += sl[j] >= 0;
-            if (atomicAdd(&p.arrive[c - nbody], 1) != k - 1) break;
-            __threadfence();
+            int* ctr = p.arrive + (c - nbody);
+            if (from_body) {
+                if (arrive_relaxed(ctr) != k - 1) break;
+                fence_acquire();
+            } else {
+                if (arrive_acq_rel(ctr) != k - 1) break;
+            }
             int comp[8];
+            float4 kq[8];
             int used = 0, cnt = 0;
             float cm = 0.0f, sx = 0.0f, sy = 0.0f, sz = 0.0f;
             double dm = 0.0, dx = 0.0, dy = 0.0, dz = 0.0;
@@ -271,7 +308,12 @@ __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
                 const int ch = sl[j];
                 if (ch < 0) continue;
                 const float4 q = ld_cg4(p.node4 + ch);
-                cnt += ch >= nbody ? __ldcg(p.count + (ch - nbody)) : 1;
+                if (ch >= nbody) {
+                    p.loff[ch - nbody] = cnt;
+                    cnt += __ldcg(p.count + (ch - nbody));
+                } else {
+                    cnt += 1;
+                }
                 if (froot) {
                     dm += (double)q.w;
                     dx += (double)q.x * (double)q.w;
@@ -283,13 +325,20 @@ __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
                     sy = madd<REF>(q.y, q.w, sy);
                     sz = madd<REF>(q.z, q.w, sz);
                 }
+                kq[used] = q;
                 comp[used++] = ch;
             }
 #pragma unroll
             for (int j = 0; j < 8; ++j)
-                if (j >= used) comp[j] = kNull;
+                if (j >= used) {
+                    comp[j] = kNull;
+                    kq[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
             reinterpret_cast<int4*>(ch8)[0] = make_int4(comp[0], comp[1], comp[2], comp[3]);
             reinterpret_cast<int4*>(ch8)[1] = make_int4(comp[4], comp[5], comp[6], comp[7]);
+            float4* kb = p.kids4 + ((size_t)(c - nbody) << 3);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) kb[j] = kq[j];
             p.count[c - nbody] = cnt;
             if (froot) {
                 p.node4[c] = make_float4((float)(dx / dm), (float)(dy / dm), (float)(dz / dm), (float)dm);
@@ -297,42 +346,46 @@ __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
                 const float inv = __fdiv_rn(1.0f, cm);
                 p.node4[c] = make_float4(__fmul_rn(sx, inv), __fmul_rn(sy, inv), __fmul_rn(sz, inv), cm);
             }
-            __threadfence();
             const int pc = p.parent[c];
             if (pc >= 0 && pc <= c) {   // parents always have higher indices
                 raise_error(p.st, NBH_ERR_STATE);
                 break;
             }
             c = pc;
+            from_body = false;
         }
     }
 }
 
 // -------------------------------------------------------------------------------------
-// Sort (sort.cl:24-75).  Cells from the top of the pool downward; each waits (bounded)
-// until its parent has given it a start offset, then hands consecutive offsets to its
-// child cells in child order and places its body children.  Parents have higher indices
-// than their children and every thread of the (fully resident) grid walks its cells in
-// decreasing order, so every wait ends.
+// Sort (sort.cl:24-75): bodies in depth-first octant order.  A cell's first position is
+// its universe's first position plus the offsets (loff, from summarize) of the cell and
+// of each ancestor inside its parent's range -- the sum sort.cl:44-58 accumulates from
+// the root down.  Each cell walks up to its root to form that sum (no thread waits for
+// another), records it in start[], and places its body children: in child order, a cell
+// child advances the position by its body count, a body child takes the next position.
 __global__ void __launch_bounds__(256) sort_kernel(StepParams p) {
     if (load_status(p.st)) return;
     const int nbody = p.nbody;
     const int bottom = p.st->bottom;
     const int stride = gridDim.x * blockDim.x;
-    for (int c = p.nnodes - (int)(blockIdx.x * blockDim.x + threadIdx.x); c >= bottom; c -= stride) {
-        int s = ld_relaxed(p.start + (c - nbody));
-        if (s < 0) {
-            const unsigned long long t0 = global_ns();
-            do {
-                __nanosleep(32);
-                if (load_status(p.st)) return;
-                if (global_ns() - t0 > kWaitNs) {
-                    raise_error(p.st, NBH_ERR_TIMEOUT);
-                    return;
-                }
-                s = ld_relaxed(p.start + (c - nbody));
-            } while (s < 0);
+    for (int c = bottom + (int)(blockIdx.x * blockDim.x + threadIdx.x); c <= p.nnodes; c += stride) {
+        int s = 0;
+        int x = c;
+        for (int guard = 0;; ++guard) {
+            const int px = p.parent[x];
+            if (px < 0) {
+                s += p.start[x - nbody];         // a root: its universe's first position
+                break;
+            }
+            if (px <= x || guard > kMaxDepth) {  // parents have higher indices; depth <= 64
+                raise_error(p.st, NBH_ERR_STATE);
+                return;
+            }
+            s += p.loff[x - nbody];
+            x = px;
         }
+        if (x != c) p.start[c - nbody] = s;
         const int* ch8 = cell_child(p, c);
         const int4 s0 = reinterpret_cast<const int4*>(ch8)[0];
         const int4 s1 = reinterpret_cast<const int4*>(ch8)[1];
@@ -340,12 +393,8 @@ __global__ void __launch_bounds__(256) sort_kernel(StepParams p) {
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int ch = sl[j];
-            if (ch >= nbody) {
-                st_release(p.start + (ch - nbody), s);
-                s += p.count[ch - nbody];
-            } else if (ch >= 0) {
-                p.sorted[s++] = ch;
-            }
+            if (ch >= nbody) s += p.count[ch - nbody];
+            else if (ch >= 0) p.sorted[s++] = ch;
         }
     }
 }
@@ -357,6 +406,9 @@ void launch_bbox(const StepParams& p, int grid, cudaStream_t s) {
 }
 void launch_build(const StepParams& p, int grid, cudaStream_t s) {
     build_kernel<<<grid, 256, 0, s>>>(p);
+}
+void launch_link(const StepParams& p, int grid, cudaStream_t s) {
+    link_kernel<<<grid, 256, 0, s>>>(p);
 }
 void launch_summarize(const StepParams& p, bool ref, int grid, cudaStream_t s) {
     if (ref) {
