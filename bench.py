@@ -363,6 +363,7 @@ def main():
             "gint_per_s_force_only": inter_ts / (force_ms * 1e-3) / 1e9,
             "interactions_per_step": interactions,
             "max_depth": int(st["max_depth"]), "cells": cells,
+            "build_contention": {"lock_waits": int(st["lock_waits"]), "cas_misses": int(st["cas_misses"])},
             "force_error": force_error,
             "stage_ms": {k[3:]: v for k, v in acc.items()},
             "stages": stages,

@@ -537,6 +537,10 @@ int nbh_get_stats(nbh_sim* sim, nbh_stats* out) {
     out->max_depth = d.max_depth;
     out->cells = d.bottom > 0 ? (sim->nnodes + 1 - d.bottom) : 0;
     out->status = d.status;
+    for (int j = 0; j < kDiagSlots; ++j) {
+        out->lock_waits += d.lock_waits[j];
+        out->cas_misses += d.cas_misses[j];
+    }
     out->ms_bbox = sim->stage_ms[0];
     out->ms_build = sim->stage_ms[1];
     out->ms_summarize = sim->stage_ms[2];

@@ -32,6 +32,18 @@ constexpr int kMaxDepth = NBH_MAXDEPTH;
 // NBH_ERR_TIMEOUT and returns (the reference's spin-waits have no bound).
 constexpr unsigned long long kWaitNs = 4000000000ull;
 
+// Back-off of a descent that finds its slot locked: starts at kBackoffMinNs and doubles up
+// to kBackoffMaxNs (compile-time tunables).
+#ifndef NBH_BACKOFF_MIN_NS
+#define NBH_BACKOFF_MIN_NS 64
+#endif
+#ifndef NBH_BACKOFF_MAX_NS
+#define NBH_BACKOFF_MAX_NS 64
+#endif
+constexpr unsigned kBackoffMinNs = NBH_BACKOFF_MIN_NS;
+constexpr unsigned kBackoffMaxNs = NBH_BACKOFF_MAX_NS;
+constexpr int kDiagSlots = 32;
+
 struct DevState {
     int status;          // NBH_OK or the first NBH_ERR_* raised by a stage
     int bottom;          // lowest allocated cell (reference _bottom)
@@ -39,10 +51,14 @@ struct DevState {
     int step;            // reference _step: -1 after load, incremented by the bbox stage
     int bbox_ticket;     // last-block ticket of the bbox stage (reference _blockCount)
     int force_next;      // work counter of the force stage
-    int sort_next;       // unused, reserved
     int pad0;
+    int pad1;
     unsigned long long interactions;   // accepted force evaluations of the last step
-    unsigned long long pad1[3];
+    unsigned long long pad2[3];
+    // Build contention meters, spread over kDiagSlots addresses so that counting does not
+    // itself serialise: descents that found their slot locked, and lost lock races.
+    int lock_waits[32];
+    int cas_misses[32];
 };
 
 // Read-only per-step parameters (passed by value).

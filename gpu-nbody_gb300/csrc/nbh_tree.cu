@@ -113,6 +113,7 @@ __global__ void __launch_bounds__(256) bbox_kernel(StepParams p) {
         st->bbox_ticket = 0;
         st->step += 1;
         st->force_next = 0;
+        for (int j = 0; j < kDiagSlots; ++j) st->lock_waits[j] = st->cas_misses[j] = 0;
         st->interactions = 0ull;
     }
 }
@@ -129,6 +130,7 @@ __global__ void __launch_bounds__(256) bbox_kernel(StepParams p) {
 __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
     if (load_status(p.st)) return;
     int local_max = 1;
+    int waits = 0, misses = 0;
     const int nbody = p.nbody;
     for (int ci = blockIdx.x; ci < p.nchunks; ci += gridDim.x) {
         const int4 ck = p.chunks[ci];
@@ -143,8 +145,15 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
             int path = octant(cx, cy, cz, bp.x, bp.y, bp.z);
             int* slot = cell_child(p, node) + path;
             unsigned long long t0 = 0;
+            unsigned backoff = kBackoffMinNs;
+            // Slots are read through L1.  A slot that holds a cell index keeps it for the
+            // rest of the build, and each cell's slots are one 32-byte sector first read
+            // after the cell was published, so a cell index read from L1 is always right;
+            // any other value is only acted on through the CAS below, which fails if it is
+            // stale and returns the current value.  This keeps the 1M descents off the L2
+            // lines of the top cells.
+            int ch = __ldca(slot);
             for (;;) {
-                int ch = ld_relaxed(slot);
                 while (ch >= nbody) {                      // :77-89
                     if (ch >= node || depth >= kMaxDepth) {  // children sit below parents
                         raise_error(p.st, NBH_ERR_DEPTH);
@@ -161,9 +170,10 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
                     r = h;
                     path = octant(cx, cy, cz, bp.x, bp.y, bp.z);
                     slot = cell_child(p, node) + path;
-                    ch = ld_relaxed(slot);
+                    ch = __ldca(slot);
                 }
-                if (ch != kLock && atomicCAS(slot, ch, kLock) == ch) {
+                int seen = kLock;
+                if (ch != kLock && (seen = atomicCAS(slot, ch, kLock)) == ch) {
                     if (ch == kNull) {
                         // nothing but the index itself is published: no fence needed
                         st_relaxed(slot, b);
@@ -177,7 +187,15 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
                                 raise_error(p.st, NBH_ERR_DEPTH);
                                 goto finish;
                             }
-                            const int cell = atomicSub(&p.st->bottom, 1) - 1;
+                            // Cells of the lanes splitting together come from one atomic on
+                            // the shared counter (contiguous, still below every parent).
+                            const unsigned act = __activemask();
+                            const int lane = threadIdx.x & 31;
+                            const int leader = __ffs(act) - 1;
+                            int base = 0;
+                            if (lane == leader) base = atomicSub(&p.st->bottom, __popc(act));
+                            base = __shfl_sync(act, base, leader);
+                            const int cell = base - 1 - __popc(act & ((1u << lane) - 1u));
                             if (cell <= nbody) {
                                 raise_error(p.st, NBH_ERR_POOL);
                                 goto finish;
@@ -209,6 +227,12 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
                     local_max = max(local_max, depth);
                     break;
                 }
+                if (seen != kLock) {        // the slot moved on: continue from its value
+                    if (ch != kLock) ++misses;
+                    ch = seen;
+                    continue;
+                }
+                // the slot is locked by a split in progress: wait (bounded), re-read from L2
                 if (load_status(p.st)) goto finish;
                 const unsigned long long now = global_ns();
                 if (t0 == 0) t0 = now;
@@ -216,13 +240,20 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
                     raise_error(p.st, NBH_ERR_TIMEOUT);
                     goto finish;
                 }
-                __nanosleep(64);
+                // back off exponentially: thousands of descents may wait on the same few
+                // slots near the root early in the build
+                ++waits;
+                __nanosleep(backoff);
+                backoff = min(backoff * 2, kBackoffMaxNs);
+                ch = ld_relaxed(slot);
             }
         }
     }
 finish:
     // :199; the maximum persists across steps, so the atomic is rarely needed
     if (local_max > ld_relaxed(&p.st->max_depth)) atomicMax(&p.st->max_depth, local_max);
+    if (waits) atomicAdd(&p.st->lock_waits[blockIdx.x % kDiagSlots], waits);
+    if (misses) atomicAdd(&p.st->cas_misses[blockIdx.x % kDiagSlots], misses);
 }
 
 // -------------------------------------------------------------------------------------

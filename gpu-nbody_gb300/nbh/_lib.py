@@ -49,6 +49,7 @@ class NbhStats(C.Structure):
         ("steps", C.c_int64), ("interactions", C.c_int64),
         ("max_depth", C.c_int32), ("cells", C.c_int32), ("nuniverses", C.c_int32),
         ("nbodies", C.c_int32), ("pool_nodes", C.c_int32), ("status", C.c_int32),
+        ("lock_waits", C.c_int32), ("cas_misses", C.c_int32),
         ("ms_bbox", C.c_float), ("ms_build", C.c_float), ("ms_summarize", C.c_float),
         ("ms_sort", C.c_float), ("ms_force", C.c_float), ("ms_integrate", C.c_float),
         ("ms_step", C.c_float), ("reserved", C.c_float * 8),

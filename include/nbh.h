@@ -99,6 +99,8 @@ typedef struct nbh_stats {
     int32_t nbodies;           /* total over universes */
     int32_t pool_nodes;        /* NUMBER_OF_NODES of the shared pool */
     int32_t status;            /* device status word of the last step (NBH_OK or NBH_ERR_*) */
+    int32_t lock_waits;        /* build of the last step: descents that found their slot locked */
+    int32_t cas_misses;        /* build of the last step: lock attempts that lost the race */
     /* per-stage device milliseconds of the last step (stage_timing = 1 only) */
     float   ms_bbox, ms_build, ms_summarize, ms_sort, ms_force, ms_integrate, ms_step;
     float   reserved[8];
