@@ -8,6 +8,7 @@
 // status word is read once per nbh_step call.
 #include "nbh_common.cuh"
 #include "nbh_kernels.h"
+#include "nbh_theta.h"
 
 #include <algorithm>
 #include <cmath>
@@ -31,6 +32,8 @@ struct nbh_sim {
     float4* kids4 = nullptr;
     int *child = nullptr, *count = nullptr, *start = nullptr, *arrive = nullptr, *parent = nullptr;
     int* loff = nullptr;
+    int* clevel = nullptr;
+    float4* probe = nullptr;
     int* sorted = nullptr;
     DevState* st = nullptr;
     int* ubody = nullptr;
@@ -40,7 +43,11 @@ struct nbh_sim {
     int2* warps = nullptr;
     float* staging = nullptr;      // 10 * nbody floats: x y z vx vy vz ax ay az m
     float* theta_body = nullptr;   // nbody floats when a per-body theta is active
-    bool theta_active = false;
+    bool theta_active = false;     // learned opening angle on
+    ThetaDev* model = nullptr;     // installed model (device)
+    float* model_prm = nullptr;    // its FP32 parameters (device)
+    float* probe_theta = nullptr;  // per-body theta of the last force probe (device)
+    float* feat = nullptr;         // features of every body (device, nbody * 12)
     int nchunks = 0, nwarps = 0;
     std::vector<int> h_ubody;
     // launch geometry
@@ -94,13 +101,15 @@ int grow(nbh_sim* sim, T** ptr, size_t count, size_t* cap_unused = nullptr) {
 }
 
 void free_buffers(nbh_sim* sim) {
-    void* ptrs[] = {sim->loff, sim->kids4, sim->node4, sim->vel, sim->acc, sim->kpos, sim->kvel, sim->child, sim->count,
+    void* ptrs[] = {sim->probe_theta, sim->feat, sim->clevel, sim->probe, sim->loff, sim->kids4, sim->node4, sim->vel, sim->acc, sim->kpos, sim->kvel, sim->child, sim->count,
                     sim->start, sim->arrive, sim->parent, sim->sorted, sim->ubody, sim->ubox,
                     sim->uradius, sim->chunks, sim->warps, sim->staging, sim->theta_body};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     sim->kids4 = sim->node4 = sim->vel = sim->acc = sim->kpos = sim->kvel = nullptr;
-    sim->child = sim->count = sim->start = sim->arrive = sim->parent = sim->sorted = sim->loff = nullptr;
+    sim->child = sim->count = sim->start = sim->arrive = sim->parent = sim->sorted = sim->loff = sim->clevel = nullptr;
+    sim->probe = nullptr;
+    sim->probe_theta = sim->feat = nullptr;
     sim->ubody = nullptr;
     sim->ubox = nullptr;
     sim->uradius = nullptr;
@@ -116,7 +125,7 @@ void drop_graph(nbh_sim* sim) {
     sim->exec = nullptr;
 }
 
-StepParams params(const nbh_sim* sim) {
+StepParams step_params(const nbh_sim* sim) {
     StepParams p{};
     p.node4 = sim->node4;
     p.vel = sim->vel;
@@ -127,6 +136,7 @@ StepParams params(const nbh_sim* sim) {
     p.kids4 = sim->kids4;
     p.count = sim->count;
     p.loff = sim->loff;
+    p.clevel = sim->clevel;
     p.start = sim->start;
     p.arrive = sim->arrive;
     p.parent = sim->parent;
@@ -154,7 +164,7 @@ StepParams params(const nbh_sim* sim) {
 
 // Enqueue the six stages of one step (GPUBarnesHutNBodySimulation.java:258-263).
 void enqueue_step(nbh_sim* sim, bool timed) {
-    const StepParams p = params(sim);
+    const StepParams p = step_params(sim);
     const bool ref = sim->cfg.arith == NBH_ARITH_REFERENCE;
     cudaStream_t s = sim->stream;
     if (timed) cudaEventRecord(sim->ev[0], s);
@@ -166,11 +176,36 @@ void enqueue_step(nbh_sim* sim, bool timed) {
     launch_summarize(p, ref, sim->grid_sum, s);
     if (timed) cudaEventRecord(sim->ev[3], s);
     launch_sort(p, sim->grid_sort, s);
+    if (sim->theta_active) launch_theta(p, sim->model, sim->theta_body, sim->grid_force, s);
     if (timed) cudaEventRecord(sim->ev[4], s);
-    launch_force(p, sim->cfg.vote_width, ref, sim->grid_force, s);
+    launch_force(p, sim->cfg.vote_width, ref, sim->theta_active, sim->grid_force, s);
     if (timed) cudaEventRecord(sim->ev[5], s);
     launch_integrate(p, ref, sim->grid_int, s);
     if (timed) cudaEventRecord(sim->ev[6], s);
+}
+
+// The tree stages alone (for probes and features on the current positions).  The bbox
+// stage advances the step counter; the caller restores it.
+void enqueue_tree(nbh_sim* sim, const StepParams& p) {
+    const bool ref = sim->cfg.arith == NBH_ARITH_REFERENCE;
+    cudaStream_t s = sim->stream;
+    launch_bbox(p, sim->grid_bbox, s);
+    launch_build(p, sim->grid_build, s);
+    launch_link(p, sim->grid_sum, s);
+    launch_summarize(p, ref, sim->grid_sum, s);
+    launch_sort(p, sim->grid_sort, s);
+}
+
+// Rebuild the tree of the current positions without advancing the step counter.
+int rebuild_tree(nbh_sim* sim, const StepParams& p) {
+    enqueue_tree(sim, p);
+    CK(cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    if (sim->h_state->status != NBH_OK) return fail(sim, sim->h_state->status, "tree build failed");
+    const int restored = sim->h_state->step - 1;
+    CK(cudaMemcpyAsync(&sim->st->step, &restored, sizeof(int), cudaMemcpyHostToDevice, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    return NBH_OK;
 }
 
 int build_graph(nbh_sim* sim) {
@@ -234,6 +269,10 @@ int alloc_for(nbh_sim* sim, int nbody, int nuniv, int nnodes, int nchunks, int n
     if ((e = grow(sim, &sim->kids4, (size_t)8 * ncells))) return e;
     if ((e = grow(sim, &sim->count, (size_t)ncells))) return e;
     if ((e = grow(sim, &sim->loff, (size_t)ncells))) return e;
+    if ((e = grow(sim, &sim->clevel, (size_t)ncells))) return e;
+    if ((e = grow(sim, &sim->probe, (size_t)nbody))) return e;
+    if ((e = grow(sim, &sim->probe_theta, (size_t)nbody))) return e;
+    if ((e = grow(sim, &sim->feat, (size_t)nbody * kMlpIn))) return e;
     if ((e = grow(sim, &sim->start, (size_t)ncells))) return e;
     if ((e = grow(sim, &sim->arrive, (size_t)ncells))) return e;
     if ((e = grow(sim, &sim->parent, (size_t)nnodes + 1))) return e;
@@ -337,6 +376,8 @@ int nbh_destroy(nbh_sim* sim) {
     drop_graph(sim);
     free_buffers(sim);
     if (sim->st) cudaFree(sim->st);
+    if (sim->model) cudaFree(sim->model);
+    if (sim->model_prm) cudaFree(sim->model_prm);
     if (sim->h_state) cudaFreeHost(sim->h_state);
     for (auto& ev : sim->ev)
         if (ev) cudaEventDestroy(ev);
@@ -674,6 +715,213 @@ int nbh_direct_f64(nbh_sim* sim, int32_t nidx, const int32_t* idx, double* ax, d
         ay[t] = out[3 * t + 1];
         az[t] = out[3 * t + 2];
     }
+    return NBH_OK;
+}
+
+// ---- learned opening angle -----------------------------------------------------------
+
+int nbh_set_theta_model(nbh_sim* sim, const float* params, int32_t nparams, const float* feat_mean,
+                        const float* feat_inv_std, float theta_min, float theta_max, int32_t enable) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_set_theta_model before nbh_load");
+    CK(cudaSetDevice(sim->device));
+    if (!enable) {
+        sim->theta_active = false;
+        drop_graph(sim);
+        return NBH_OK;
+    }
+    if (!params || nparams != kMlpParams || !feat_mean || !feat_inv_std || !(theta_min > 0.0f) ||
+        !(theta_max >= theta_min))
+        return fail(sim, NBH_ERR_MODEL, "model needs 4993 parameters, 12 means and inverse deviations, "
+                                        "0 < theta_min <= theta_max");
+    for (int i = 0; i < kMlpParams; ++i)
+        if (!std::isfinite(params[i])) return fail(sim, NBH_ERR_MODEL, "non-finite model parameter");
+    cudaStream_t s = sim->stream;
+    if (!sim->model) CK(cudaMalloc(reinterpret_cast<void**>(&sim->model), sizeof(ThetaDev)));
+    if (!sim->model_prm) CK(cudaMalloc(reinterpret_cast<void**>(&sim->model_prm), sizeof(float) * kMlpParams));
+    CK(cudaMemcpyAsync(sim->model_prm, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, s));
+    launch_model_convert(sim->model_prm, sim->model, s);
+    CK(cudaMemcpyAsync(sim->model->mean, feat_mean, sizeof(float) * kMlpIn, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(sim->model->inv_std, feat_inv_std, sizeof(float) * kMlpIn, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(&sim->model->theta_min, &theta_min, sizeof(float), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(&sim->model->theta_max, &theta_max, sizeof(float), cudaMemcpyHostToDevice, s));
+    // The step after switching on walks with the fixed theta (recording the error bound the
+    // features need); the model takes over from the step after that.
+    CK(cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const int since = sim->h_state->step + 1;
+    CK(cudaMemcpyAsync(&sim->st->theta_since, &since, sizeof(int), cudaMemcpyHostToDevice, s));
+    const StepParams p = step_params(sim);
+    std::vector<float> th((size_t)sim->nbody, std::sqrt(p.theta2));
+    CK(cudaMemcpyAsync(sim->theta_body, th.data(), sizeof(float) * sim->nbody, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+    sim->theta_active = true;
+    drop_graph(sim);
+    return NBH_OK;
+}
+
+int nbh_read_theta(nbh_sim* sim, float* theta) {
+    if (!sim || !theta) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_read_theta before nbh_load");
+    CK(cudaSetDevice(sim->device));
+    CK(cudaMemcpyAsync(theta, sim->theta_body, sizeof(float) * sim->nbody, cudaMemcpyDeviceToHost, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    return NBH_OK;
+}
+
+int nbh_force_probe(nbh_sim* sim, const float* theta_body, float* ax, float* ay, float* az, float* ebound,
+                    int64_t* interactions) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_force_probe before nbh_load");
+    CK(cudaSetDevice(sim->device));
+    cudaStream_t s = sim->stream;
+    const int n = sim->nbody;
+    StepParams p = step_params(sim);
+    if (theta_body) {
+        for (int i = 0; i < n; ++i)
+            if (!(theta_body[i] >= 0.0f) || !std::isfinite(theta_body[i]))
+                return fail(sim, NBH_ERR_INVALID, "per-body theta must be finite and >= 0");
+        CK(cudaMemcpyAsync(sim->probe_theta, theta_body, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    } else {
+        std::vector<float> th((size_t)n, std::sqrt(p.theta2));
+        CK(cudaMemcpyAsync(sim->probe_theta, th.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    }
+    int e;
+    p.theta_body = nullptr;
+    if ((e = rebuild_tree(sim, p))) return e;
+    p.theta_body = sim->probe_theta;
+    p.probe = sim->probe;
+    const int zero = 0;
+    const unsigned long long z64 = 0;
+    CK(cudaMemcpyAsync(&sim->st->force_next, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(&sim->st->interactions, &z64, sizeof(z64), cudaMemcpyHostToDevice, s));
+    launch_force(p, sim->cfg.vote_width, sim->cfg.arith == NBH_ARITH_REFERENCE, true, sim->grid_force, s);
+    CK(cudaGetLastError());
+    std::vector<float4> out((size_t)n);
+    CK(cudaMemcpyAsync(out.data(), sim->probe, sizeof(float4) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (sim->h_state->status != NBH_OK) return fail(sim, sim->h_state->status, "force probe failed");
+    for (int i = 0; i < n; ++i) {
+        if (ax) ax[i] = out[i].x;
+        if (ay) ay[i] = out[i].y;
+        if (az) az[i] = out[i].z;
+        if (ebound) ebound[i] = out[i].w;
+    }
+    if (interactions) *interactions = (int64_t)sim->h_state->interactions;
+    return NBH_OK;
+}
+
+int nbh_theta_features(nbh_sim* sim, float* feat, int32_t use_probe) {
+    if (!sim || !feat) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_theta_features before nbh_load");
+    CK(cudaSetDevice(sim->device));
+    cudaStream_t s = sim->stream;
+    StepParams p = step_params(sim);
+    int e;
+    if (!use_probe) {
+        p.theta_body = nullptr;
+        if ((e = rebuild_tree(sim, p))) return e;
+    }
+    if (!sim->model) {
+        CK(cudaMalloc(reinterpret_cast<void**>(&sim->model), sizeof(ThetaDev)));
+        CK(cudaMemsetAsync(sim->model, 0, sizeof(ThetaDev), s));
+    }
+    launch_features(p, sim->model, use_probe ? sim->probe : sim->acc, use_probe ? sim->probe_theta : sim->theta_body,
+                    sim->feat, std::max(1, std::min((sim->nbody + 255) / 256, 8 * sim->sms)), s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(feat, sim->feat, sizeof(float) * kMlpIn * sim->nbody, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return NBH_OK;
+}
+
+// ---- training of the model (FP32, on the device) ---------------------------------------
+
+namespace {
+struct TrainBufs {
+    float *X = nullptr, *T = nullptr, *prm = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr, *loss = nullptr;
+    MlpWork w{};
+    ~TrainBufs() {
+        void* ptrs[] = {X, T, prm, grad, m1, m2, loss, w.H1, w.H2, w.Y, w.dH1, w.dH2, w.dY};
+        for (void* q : ptrs)
+            if (q) cudaFree(q);
+    }
+};
+
+int train_setup(TrainBufs& b, const float* params, const float* X, const float* T, int n) {
+    nbh_sim* sim = nullptr;
+    std::vector<float> xt((size_t)kMlpIn * n);   // feature-major for the kernels
+    for (int s = 0; s < n; ++s)
+        for (int k = 0; k < kMlpIn; ++k) xt[(size_t)k * n + s] = X[(size_t)s * kMlpIn + k];
+    CK(cudaMalloc(reinterpret_cast<void**>(&b.X), sizeof(float) * xt.size()));
+    CK(cudaMalloc(reinterpret_cast<void**>(&b.T), sizeof(float) * n));
+    CK(cudaMalloc(reinterpret_cast<void**>(&b.prm), sizeof(float) * kMlpParams));
+    CK(cudaMalloc(reinterpret_cast<void**>(&b.grad), sizeof(float) * kMlpParams));
+    CK(cudaMalloc(reinterpret_cast<void**>(&b.m1), sizeof(float) * kMlpParams));
+    CK(cudaMalloc(reinterpret_cast<void**>(&b.m2), sizeof(float) * kMlpParams));
+    CK(cudaMalloc(reinterpret_cast<void**>(&b.loss), sizeof(float)));
+    float** acts[] = {&b.w.H1, &b.w.H2, &b.w.dH1, &b.w.dH2};
+    for (float** a : acts) CK(cudaMalloc(reinterpret_cast<void**>(a), sizeof(float) * kMlpHid * n));
+    CK(cudaMalloc(reinterpret_cast<void**>(&b.w.Y), sizeof(float) * n));
+    CK(cudaMalloc(reinterpret_cast<void**>(&b.w.dY), sizeof(float) * n));
+    CK(cudaMemcpy(b.X, xt.data(), sizeof(float) * xt.size(), cudaMemcpyHostToDevice));
+    if (T) CK(cudaMemcpy(b.T, T, sizeof(float) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b.prm, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice));
+    CK(cudaMemset(b.m1, 0, sizeof(float) * kMlpParams));
+    CK(cudaMemset(b.m2, 0, sizeof(float) * kMlpParams));
+    return NBH_OK;
+}
+}  // namespace
+
+int nbh_mlp_forward(int32_t device, const float* params, const float* X, int32_t n, float* y) {
+    nbh_sim* sim = nullptr;
+    if (!params || !X || !y || n < 1) return fail(nullptr, NBH_ERR_INVALID, "bad arguments");
+    CK(cudaSetDevice(device));
+    TrainBufs b;
+    int e;
+    if ((e = train_setup(b, params, X, nullptr, n))) return e;
+    mlp_forward(b.prm, b.X, n, b.w, nullptr);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(y, b.w.Y, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    return NBH_OK;
+}
+
+int nbh_mlp_grad(int32_t device, const float* params, const float* X, const float* T, int32_t n, float quantile,
+                 float* grad, float* loss) {
+    nbh_sim* sim = nullptr;
+    if (!params || !X || !T || !grad || n < 1 || !(quantile > 0.0f && quantile < 1.0f))
+        return fail(nullptr, NBH_ERR_INVALID, "bad arguments");
+    CK(cudaSetDevice(device));
+    TrainBufs b;
+    int e;
+    if ((e = train_setup(b, params, X, T, n))) return e;
+    mlp_grad(b.prm, b.X, b.T, n, quantile, b.w, b.grad, b.loss, nullptr);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(grad, b.grad, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost));
+    if (loss) CK(cudaMemcpy(loss, b.loss, sizeof(float), cudaMemcpyDeviceToHost));
+    return NBH_OK;
+}
+
+int nbh_mlp_train(int32_t device, float* params, const float* X, const float* T, int32_t n, float quantile,
+                  int32_t iters, float lr, float* loss) {
+    nbh_sim* sim = nullptr;
+    if (!params || !X || !T || n < 1 || iters < 0 || !(quantile > 0.0f && quantile < 1.0f) || !(lr > 0.0f))
+        return fail(nullptr, NBH_ERR_INVALID, "bad arguments");
+    CK(cudaSetDevice(device));
+    TrainBufs b;
+    int e;
+    if ((e = train_setup(b, params, X, T, n))) return e;
+    cudaStream_t s = nullptr;
+    for (int it = 1; it <= iters; ++it) {
+        mlp_grad(b.prm, b.X, b.T, n, quantile, b.w, b.grad, b.loss, s);
+        adam_step(b.prm, b.grad, b.m1, b.m2, lr, it, s);
+    }
+    // loss of the final parameters
+    mlp_grad(b.prm, b.X, b.T, n, quantile, b.w, b.grad, b.loss, s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(params, b.prm, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost));
+    if (loss) CK(cudaMemcpy(loss, b.loss, sizeof(float), cudaMemcpyDeviceToHost));
     return NBH_OK;
 }
 

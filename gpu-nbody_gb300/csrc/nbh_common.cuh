@@ -14,8 +14,9 @@
 //             int    child[8k .. 8k+7]  child slots, -1 empty, -2 locked (buildtree.cl:7-8)
 //             float4 kids4[8k .. 8k+7]  copies of the children's node records, in slot
 //                                       order, written by summarize for the force walk
-//             int    count[k], start[k], loff[k], arrive[k]
-// Per body:   float4 vel[b], acc[b]  (w unused), sorted[s] = body at depth-first position s
+//             int    count[k], start[k], loff[k], arrive[k], clevel[k]
+// Per body:   float4 vel[b], acc[b] (w: quadrupole error bound of the last force walk when
+//             the learned opening angle is on), sorted[s] = body at depth-first position s
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -51,7 +52,7 @@ struct DevState {
     int step;            // reference _step: -1 after load, incremented by the bbox stage
     int bbox_ticket;     // last-block ticket of the bbox stage (reference _blockCount)
     int force_next;      // work counter of the force stage
-    int pad0;
+    int theta_since;     // learned theta: steps up to this index use the fixed theta
     int pad1;
     unsigned long long interactions;   // accepted force evaluations of the last step
     unsigned long long pad2[3];
@@ -74,6 +75,8 @@ struct StepParams {
     int* start;          // ncells: first depth-first position of each cell
     int* loff;           // ncells: offset of a cell inside its parent's depth-first range
     int* arrive;         // ncells
+    int* clevel;         // ncells: tree level of each cell (root = 0)
+    float4* probe;       // nbody: force-probe output (x, y, z, error bound), or null
     int* parent;         // nnodes + 1
     int* sorted;         // nbody
     const float* theta_body;   // per-body theta, or null for fixed theta

@@ -33,9 +33,13 @@ __device__ __forceinline__ float rsqrt_ftz(float x) {
     return y;
 }
 
-template <bool REF>
+// One accepted interaction (calculateforce.cl:146-151).  With FEAT it also accumulates
+// the quadrupole error bound m s^2 / d^4 of an accepted cell of full width^2 s2 (0 for a
+// body), the feature the learned opening angle is predicted from.
+template <bool REF, bool FEAT>
 __device__ __forceinline__ void interact(const float4 q, const float dx, const float dy, const float dz,
-                                         const float d2, float& ax, float& ay, float& az) {
+                                         const float d2, float& ax, float& ay, float& az, float& eb,
+                                         const float s2) {
     float rd;
     if constexpr (REF) rd = __fdiv_rn(1.0f, __fsqrt_rn(d2));
     else rd = rsqrt_ftz(d2);
@@ -43,6 +47,7 @@ __device__ __forceinline__ void interact(const float4 q, const float dx, const f
     ax = madd<REF>(dx, f, ax);
     ay = madd<REF>(dy, f, ay);
     az = madd<REF>(dz, f, az);
+    if constexpr (FEAT) eb = __fadd_rn(eb, __fmul_rn(__fmul_rn(f, rd), s2));
 }
 
 template <bool REF>
@@ -74,8 +79,10 @@ __device__ __forceinline__ float dist2(const float dx, const float dy, const flo
 // acceleration store (:183-185).
 //
 // REF: reference arithmetic (rounded products, 1/sqrt correctly rounded); otherwise FMA and
-// the hardware inverse square root.  PB: per-body opening angle from theta_body.
-template <int W, bool REF, bool PB>
+// the hardware inverse square root.  PB: per-body opening angle from theta_body.  FEAT:
+// also accumulate each body's quadrupole error bound into acc.w.  With p.probe set the
+// results go to p.probe (x, y, z, bound) and no body state changes (force probe).
+template <int W, bool REF, bool PB, bool FEAT>
 __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
     if (load_status(p.st)) return;
     constexpr int kGroups = kForceThreads / W;
@@ -121,7 +128,7 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
             th2 = __fmul_rn(th, th);
         }
         const float t0 = th2 > 0.0f ? __fdiv_rn(rr, th2) : rr;
-        float ax = 0.f, ay = 0.f, az = 0.f;
+        float ax = 0.f, ay = 0.f, az = 0.f, eb = 0.f;
         long long ninter = 0;
         const int root = p.nnodes - u;
 
@@ -171,7 +178,7 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
                     const float sl = __int_as_float(e.y);
                     const float dq = __fadd_rn(__fmul_rn(t0, sl), eps2);
                     if (__all_sync(gmask, d2 >= dq)) {
-                        interact<REF>(q, dx, dy, dz, d2, ax, ay, az);
+                        interact<REF, FEAT>(q, dx, dy, dz, d2, ax, ay, az, eb, __fmul_rn(rr, fmaxf(sl, 0.0f)));
                     } else {
                         open = e.x;
                         open_s = __fmul_rn(sl, 0.25f);
@@ -203,7 +210,8 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
                     const float dz = __fsub_rn(q.z, pb.z);
                     const float d2 = dist2<REF>(dx, dy, dz, eps2);
                     if (ch < nbody || __all_sync(gmask, d2 >= dq)) {
-                        interact<REF>(q, dx, dy, dz, d2, ax, ay, az);
+                        interact<REF, FEAT>(q, dx, dy, dz, d2, ax, ay, az, eb,
+                                            ch >= nbody ? ldexpf(rr, -2 * depth) : 0.0f);
                         ++ninter;
                     } else {
                         if (depth + 1 >= kMaxDepth) {   // unreachable for a tree the build accepted
@@ -222,11 +230,21 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
             }
         }
 
-        if (valid) {
+        if (valid && p.probe) {
             if (p.G != 1.0f) {
                 ax = __fmul_rn(ax, p.G);
                 ay = __fmul_rn(ay, p.G);
                 az = __fmul_rn(az, p.G);
+                eb = __fmul_rn(eb, p.G);
+            }
+            p.probe[b] = make_float4(ax, ay, az, eb);
+            my_inter += (unsigned long long)ninter;
+        } else if (valid) {
+            if (p.G != 1.0f) {
+                ax = __fmul_rn(ax, p.G);
+                ay = __fmul_rn(ay, p.G);
+                az = __fmul_rn(az, p.G);
+                eb = __fmul_rn(eb, p.G);
             }
             float4 v = p.vel[b];
             const float4 ao = p.acc[b];
@@ -248,7 +266,7 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
                 }
                 p.vel[b] = v;
             }
-            p.acc[b] = make_float4(ax, ay, az, 0.0f);
+            p.acc[b] = make_float4(ax, ay, az, eb);
             my_inter += (unsigned long long)ninter;
         }
         __syncwarp();
@@ -259,50 +277,62 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
 }
 
 // -------------------------------------------------------------------------------------
-template <int W, bool REF>
-static void launch_force_t(const StepParams& p, bool pb, int grid, cudaStream_t s) {
+template <int W, bool REF, bool PB>
+static void launch_force_pf(const StepParams& p, bool feat, int grid, cudaStream_t s) {
     constexpr size_t sm = force_smem_bytes<W>();
-    if (pb) force_kernel<W, REF, true><<<grid, kForceThreads, sm, s>>>(p);
-    else force_kernel<W, REF, false><<<grid, kForceThreads, sm, s>>>(p);
+    if (feat) force_kernel<W, REF, PB, true><<<grid, kForceThreads, sm, s>>>(p);
+    else force_kernel<W, REF, PB, false><<<grid, kForceThreads, sm, s>>>(p);
 }
 
-template <int W, bool REF, bool PB>
+template <int W, bool REF>
+static void launch_force_t(const StepParams& p, bool pb, bool feat, int grid, cudaStream_t s) {
+    if (pb) launch_force_pf<W, REF, true>(p, feat, grid, s);
+    else launch_force_pf<W, REF, false>(p, feat, grid, s);
+}
+
+template <int W, bool REF, bool PB, bool FEAT>
 static cudaError_t prep_force() {
-    return cudaFuncSetAttribute(force_kernel<W, REF, PB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(force_kernel<W, REF, PB, FEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)force_smem_bytes<W>());
+}
+
+template <int W, bool REF>
+static cudaError_t prep_force_w() {
+    cudaError_t e = cudaSuccess, t;
+    if ((t = prep_force<W, REF, false, false>()) != cudaSuccess) e = t;
+    if ((t = prep_force<W, REF, false, true>()) != cudaSuccess) e = t;
+    if ((t = prep_force<W, REF, true, false>()) != cudaSuccess) e = t;
+    if ((t = prep_force<W, REF, true, true>()) != cudaSuccess) e = t;
+    return e;
 }
 
 int prepare_force_kernels() {
     cudaError_t e = cudaSuccess, t;
-    if ((t = prep_force<32, false, false>()) != cudaSuccess) e = t;
-    if ((t = prep_force<32, false, true>()) != cudaSuccess) e = t;
-    if ((t = prep_force<32, true, false>()) != cudaSuccess) e = t;
-    if ((t = prep_force<32, true, true>()) != cudaSuccess) e = t;
-    if ((t = prep_force<16, false, false>()) != cudaSuccess) e = t;
-    if ((t = prep_force<16, false, true>()) != cudaSuccess) e = t;
-    if ((t = prep_force<16, true, false>()) != cudaSuccess) e = t;
-    if ((t = prep_force<16, true, true>()) != cudaSuccess) e = t;
+    if ((t = prep_force_w<32, false>()) != cudaSuccess) e = t;
+    if ((t = prep_force_w<32, true>()) != cudaSuccess) e = t;
+    if ((t = prep_force_w<16, false>()) != cudaSuccess) e = t;
+    if ((t = prep_force_w<16, true>()) != cudaSuccess) e = t;
     return (int)e;
 }
 
-void launch_force(const StepParams& p, int vote, bool ref, int grid, cudaStream_t s) {
+void launch_force(const StepParams& p, int vote, bool ref, bool feat, int grid, cudaStream_t s) {
     const bool pb = p.theta_body != nullptr;
     if (vote == 16) {
-        if (ref) launch_force_t<16, true>(p, pb, grid, s);
-        else launch_force_t<16, false>(p, pb, grid, s);
+        if (ref) launch_force_t<16, true>(p, pb, feat, grid, s);
+        else launch_force_t<16, false>(p, pb, feat, grid, s);
     } else {
-        if (ref) launch_force_t<32, true>(p, pb, grid, s);
-        else launch_force_t<32, false>(p, pb, grid, s);
+        if (ref) launch_force_t<32, true>(p, pb, feat, grid, s);
+        else launch_force_t<32, false>(p, pb, feat, grid, s);
     }
 }
 
 int occupancy_force(int vote, bool ref, int* blocks_per_sm) {
     const size_t s16 = force_smem_bytes<16>(), s32 = force_smem_bytes<32>();
     if (vote == 16)
-        return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, true, false>, kForceThreads, s16)
-                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, false, false>, kForceThreads, s16);
-    return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<32, true, false>, kForceThreads, s32)
-               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<32, false, false>, kForceThreads, s32);
+        return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, true, false, false>, kForceThreads, s16)
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, false, false, false>, kForceThreads, s16);
+    return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<32, true, false, false>, kForceThreads, s32)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<32, false, false, false>, kForceThreads, s32);
 }
 
 }  // namespace nbh

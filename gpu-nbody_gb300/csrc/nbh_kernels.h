@@ -11,7 +11,7 @@ void launch_build(const StepParams& p, int grid, cudaStream_t s);
 void launch_link(const StepParams& p, int grid, cudaStream_t s);
 void launch_summarize(const StepParams& p, bool ref, int grid, cudaStream_t s);
 void launch_sort(const StepParams& p, int grid, cudaStream_t s);
-void launch_force(const StepParams& p, int vote, bool ref, int grid, cudaStream_t s);
+void launch_force(const StepParams& p, int vote, bool ref, bool feat, int grid, cudaStream_t s);
 void launch_integrate(const StepParams& p, bool ref, int grid, cudaStream_t s);
 
 void launch_pack(int n, const float* soa, int mask, float4* node4, float4* vel, float4* acc, int grid,

@@ -97,6 +97,7 @@ __global__ void __launch_bounds__(256) bbox_kernel(StepParams p) {
         c4[1] = make_int4(kNull, kNull, kNull, kNull);
         p.parent[root] = -1;
         p.arrive[k] = 0;
+        p.clevel[k] = 0;
         p.count[k] = 0;
         p.start[k] = p.ubody[u];
         p.uradius[u] = radius;
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
                             reinterpret_cast<int4*>(cc)[0] = make_int4(kNull, kNull, kNull, kNull);
                             reinterpret_cast<int4*>(cc)[1] = make_int4(kNull, kNull, kNull, kNull);
                             p.arrive[cell - nbody] = 0;
-                            p.start[cell - nbody] = -1;
+                            p.clevel[cell - nbody] = depth - 1;   // root = level 0
                             if (patch < 0) patch = cell;
                             else cell_child(p, cur)[cpath] = cell;
                             const int opath = octant(cx, cy, cz, op.x, op.y, op.z);
@@ -328,12 +329,11 @@ __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
             } else {
                 if (arrive_acq_rel(ctr) != k - 1) break;
             }
-            int comp[8];
-            float4 kq[8];
             int used = 0, cnt = 0;
             float cm = 0.0f, sx = 0.0f, sy = 0.0f, sz = 0.0f;
             double dm = 0.0, dx = 0.0, dy = 0.0, dz = 0.0;
             const bool froot = PRECISE && c >= first_root;
+            float4* kb = p.kids4 + ((size_t)(c - nbody) << 3);
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const int ch = sl[j];
@@ -356,20 +356,17 @@ __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
                     sy = madd<REF>(q.y, q.w, sy);
                     sz = madd<REF>(q.z, q.w, sz);
                 }
-                kq[used] = q;
-                comp[used++] = ch;
+                // compacted slot and the child's record, at the running position
+                ch8[used] = ch;
+                kb[used] = q;
+                ++used;
             }
 #pragma unroll
             for (int j = 0; j < 8; ++j)
                 if (j >= used) {
-                    comp[j] = kNull;
-                    kq[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    ch8[j] = kNull;
+                    kb[j] = make_float4(0.f, 0.f, 0.f, 0.f);
                 }
-            reinterpret_cast<int4*>(ch8)[0] = make_int4(comp[0], comp[1], comp[2], comp[3]);
-            reinterpret_cast<int4*>(ch8)[1] = make_int4(comp[4], comp[5], comp[6], comp[7]);
-            float4* kb = p.kids4 + ((size_t)(c - nbody) << 3);
-#pragma unroll
-            for (int j = 0; j < 8; ++j) kb[j] = kq[j];
             p.count[c - nbody] = cnt;
             if (froot) {
                 p.node4[c] = make_float4((float)(dx / dm), (float)(dy / dm), (float)(dz / dm), (float)dm);

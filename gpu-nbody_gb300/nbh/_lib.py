@@ -25,6 +25,8 @@ NBH_ERR_MODEL = -9
 NBH_MAXDEPTH = 64
 NBH_ARITH_FMA = 0
 NBH_ARITH_REFERENCE = 1
+NBH_MLP_PARAMS = 4993
+NBH_MLP_FEATURES = 12
 
 ERROR_NAMES = {
     NBH_OK: "NBH_OK", NBH_ERR_INVALID: "NBH_ERR_INVALID", NBH_ERR_CUDA: "NBH_ERR_CUDA",
@@ -93,6 +95,13 @@ SIGNATURES = {
     "nbh_generate_lonlat_sphere": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32] + [_P] * 4),
     "nbh_generate_rotating_disk": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_float, C.c_float,
                                              C.c_float] + [_P] * 7),
+    "nbh_set_theta_model": (C.c_int, [_P, _P, C.c_int32, _P, _P, C.c_float, C.c_float, C.c_int32]),
+    "nbh_read_theta": (C.c_int, [_P, _P]),
+    "nbh_force_probe": (C.c_int, [_P, _P, _P, _P, _P, _P, C.POINTER(C.c_int64)]),
+    "nbh_theta_features": (C.c_int, [_P, _P, C.c_int32]),
+    "nbh_mlp_train": (C.c_int, [C.c_int32, _P, _P, _P, C.c_int32, C.c_float, C.c_int32, C.c_float, _F]),
+    "nbh_mlp_grad": (C.c_int, [C.c_int32, _P, _P, _P, C.c_int32, C.c_float, _P, _F]),
+    "nbh_mlp_forward": (C.c_int, [C.c_int32, _P, _P, C.c_int32, _P]),
     "nbh_universe_read": (C.c_int, [C.c_char_p, _I] + [_P] * 7),
     "nbh_universe_write": (C.c_int, [C.c_char_p, C.c_int32] + [_P] * 7),
 }

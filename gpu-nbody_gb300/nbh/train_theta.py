@@ -1,0 +1,110 @@
+"""Train the learned opening-angle model on the GPU and store it in nbh/models/.
+
+  python gpu-nbody_gb300/nbh/train_theta.py [--n 1048576] [--out PATH]
+
+Training data: Plummer spheres (scale radius 1, mass 1) of n bodies, two seeds, each at
+its initial state and after a few steps; per snapshot nbh.learned.collect() probes the
+force at the angle grid on sampled bodies and measures the error against the FP64 direct
+sum.  Candidate models are fitted for several error budgets tau (fractions of the fixed
+theta = 0.5 p99 error) and loss quantiles, then validated on a third seed through the
+production step path (features and BF16 inference inside the step); the candidate with the
+fewest interactions whose p99 error does not exceed the fixed-theta p99 is kept.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+import nbh  # noqa: E402
+from nbh import learned as LR  # noqa: E402
+from nbh import universe as U  # noqa: E402
+
+
+def evaluate(arrs, model, theta=0.5, eps=0.05, dt=0.01, nsample=4096, warm=2, seed=17, device=0):
+    """p99 / median relative force error against FP64 and interactions of one step, plain
+    fixed theta and (if model) learned theta, both from the same initial state."""
+    n = arrs[0].size
+    idx = np.sort(np.random.default_rng(seed).choice(n, min(nsample, n), replace=False)).astype(np.int32)
+    out = {}
+    for mode in ("plain", "learned"):
+        if mode == "learned" and model is None:
+            continue
+        with nbh.Simulation(theta=theta, eps=eps, dt=dt, device=device) as s:
+            s.load(*arrs)
+            if mode == "learned":
+                LR.install(s, model)
+            s.step(warm)
+            ref = s.direct_f64(idx)
+            s.step(1)
+            st = s.read()
+            e = LR.rel_error(st["ax"][idx], st["ay"][idx], st["az"][idx], *ref)
+            out[mode] = {"p99": float(np.percentile(e, 99)), "median": float(np.median(e)),
+                         "interactions": int(s.stats()["interactions"])}
+            if mode == "learned":
+                th = LR.read_theta(s)
+                out[mode]["theta_mean"] = float(th.mean())
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--samples", type=int, default=6144)
+    ap.add_argument("--out", default=LR.default_model_path())
+    ap.add_argument("--iters", type=int, default=1500)
+    args = ap.parse_args()
+    t0 = time.time()
+    rng = np.random.default_rng(1)
+    Es, Fs = [], []
+    for seed in (101, 102):
+        arrs = U.PlummerUniverseGenerator(seed=seed).arrays(args.n)
+        with nbh.Simulation(theta=0.5, eps=0.05, dt=0.01) as s:
+            s.load(*arrs)
+            for k in range(2):
+                if k:
+                    s.step(10)
+                E, F, I = LR.collect(s, args.samples, rng)
+                Es.append(E)
+                Fs.append(F)
+                print("snapshot seed %d part %d: p99 at theta 0.5 = %.3e, interactions %s"
+                      % (seed, k, np.percentile(E[1], 99), I.tolist()), flush=True)
+    p99_plain = float(np.median([np.percentile(E[1], 99) for E in Es]))
+    val = U.PlummerUniverseGenerator(seed=103).arrays(args.n)
+    base = evaluate(val, None)["plain"]
+    print("validation plain:", base, flush=True)
+    best = None
+    results = []
+    for tau_frac in (0.3, 0.4, 0.5, 0.7):
+        for q in (0.1, 0.2, 0.3):
+            tau = tau_frac * p99_plain
+            X = np.concatenate([F.reshape(-1, 12) for F in Fs])
+            Y = np.concatenate([np.tile(LR.theta_target(E, tau), E.shape[0]) for E in Es])
+            model = LR.train(X, Y, quantile=q, iters=args.iters)
+            model.update({"theta_min": 0.3, "theta_max": 1.0, "tau_frac": tau_frac, "tau": tau})
+            r = evaluate(val, model)["learned"]
+            r.update({"tau_frac": tau_frac, "quantile": q, "loss": model["loss"],
+                      "gain": base["interactions"] / r["interactions"], "p99_ratio": r["p99"] / base["p99"]})
+            results.append(r)
+            print(json.dumps(r), flush=True)
+            if r["p99"] <= base["p99"] and (best is None or r["interactions"] < best[1]["interactions"]):
+                best = (model, r)
+    if best is None:
+        raise SystemExit("no candidate met the fixed-theta p99 error")
+    model, r = best
+    model["validation"] = json.dumps({"plain": base, "learned": r})
+    os.makedirs(os.path.dirname(args.out), exist_ok=True)
+    LR.save(model, args.out)
+    print("saved %s: gain %.3fx interactions at p99 ratio %.3f (%.0f s)"
+          % (args.out, r["gain"], r["p99_ratio"], time.time() - t0))
+
+
+if __name__ == "__main__":
+    main()

@@ -195,6 +195,51 @@ int nbh_read_tree(nbh_sim* sim, int32_t* child, float* node4, int32_t* count,
 int nbh_direct_f64(nbh_sim* sim, int32_t nidx, const int32_t* idx,
                    double* ax, double* ay, double* az);
 
+/* ---- Learned per-body opening angle (no counterpart in the reference) ---------------- */
+
+/* Installs an MLP 12->64->64->1 (ReLU; row-major FP32 parameters W1[64][12], b1[64],
+ * W2[64][64], b2[64], W3[64], b3: NBH_MLP_PARAMS floats) and the normalisation of its 12
+ * features (mean[12], inv_std[12]).  Every step then sets each body's opening angle to
+ * clamp(exp(MLP((f - mean) * inv_std)), theta_min, theta_max), evaluated with BF16 weights
+ * on the tensor cores, and the force walk records each body's quadrupole error bound for
+ * the next step's features.  The first step after switching on walks with the fixed
+ * theta.  enable = 0 returns to the fixed theta.  Features (nbh_theta_features order):
+ * log10|a|, log10(bound/|a|), log10(theta of the last walk), log10(d/R), log10(n_leaf+1),
+ * level(leaf)/20, log10(n_leaf_parent+1), log10(n_leaf/h^3), log10(m_leaf/M),
+ * log10(|a| d^2/M), log10(eps/h), log10(h/d); d = distance to the universe's centre of
+ * mass, R, M = root half-width and mass, h = half-width of the cell holding the body. */
+#define NBH_MLP_PARAMS 4993
+#define NBH_MLP_FEATURES 12
+int nbh_set_theta_model(nbh_sim* sim, const float* params, int32_t nparams,
+                        const float* feat_mean, const float* feat_inv_std,
+                        float theta_min, float theta_max, int32_t enable);
+
+/* Writes the per-body opening angle of the last step into theta[N] (host). */
+int nbh_read_theta(nbh_sim* sim, float* theta);
+
+/* One force evaluation at the current positions (the tree is rebuilt; positions,
+ * velocities, accelerations and the step counter are left unchanged) with a per-body theta
+ * (host array, N floats; NULL = the configured fixed theta).  Writes accelerations, the
+ * per-body quadrupole error bound and the interaction count.  Training data come from this. */
+int nbh_force_probe(nbh_sim* sim, const float* theta_body,
+                    float* ax, float* ay, float* az, float* ebound, int64_t* interactions);
+
+/* Raw (unnormalised) features of every body, feat[N*12] (host).  use_probe = 1 takes the
+ * "previous walk" inputs from the last nbh_force_probe; 0 from the last step (the tree is
+ * rebuilt for the current positions). */
+int nbh_theta_features(nbh_sim* sim, float* feat, int32_t use_probe);
+
+/* Training of the model on the device with FP32 forward/backward kernels: samples X[n*12]
+ * (normalised features, row-major), targets T[n] (log theta), pinball loss at `quantile`
+ * (the fraction of samples whose target the prediction may exceed).  nbh_mlp_train runs
+ * `iters` full-batch Adam steps from params (updated in place) and reports the final loss;
+ * nbh_mlp_grad returns the gradient and loss of one pass; nbh_mlp_forward the outputs. */
+int nbh_mlp_train(int32_t device, float* params, const float* X, const float* T, int32_t n,
+                  float quantile, int32_t iters, float lr, float* loss);
+int nbh_mlp_grad(int32_t device, const float* params, const float* X, const float* T, int32_t n,
+                 float quantile, float* grad, float* loss);
+int nbh_mlp_forward(int32_t device, const float* params, const float* X, int32_t n, float* y);
+
 /* ---- Seeded universe generators (UniverseGenerator implementations) ------------------ */
 /* All fill caller arrays of n floats at offset `offset`, deterministic in `seed`.
  * Velocity pointers may be NULL where a generator leaves velocities unset. */

@@ -34,7 +34,7 @@ class _RbSim(C.Structure):
         ("ax", C.POINTER(C.c_float)), ("ay", C.POINTER(C.c_float)), ("az", C.POINTER(C.c_float)),
         ("kx", C.POINTER(C.c_float)), ("ky", C.POINTER(C.c_float)), ("kz", C.POINTER(C.c_float)),
         ("kvx", C.POINTER(C.c_float)), ("kvy", C.POINTER(C.c_float)), ("kvz", C.POINTER(C.c_float)),
-        ("theta_body", C.POINTER(C.c_float)),
+        ("theta_body", C.POINTER(C.c_float)), ("ebound", C.POINTER(C.c_float)),
         ("child", C.POINTER(C.c_int)), ("count", C.POINTER(C.c_int)),
         ("start", C.POINTER(C.c_int)), ("sorted", C.POINTER(C.c_int)),
         ("radius", C.c_float),
@@ -60,6 +60,7 @@ def lib():
         L.rb_destroy.argtypes = [P]
         L.rb_load.argtypes = [P] + [C.c_void_p] * 7
         L.rb_set_theta_body.argtypes = [P, C.c_void_p]
+        L.rb_enable_ebound.argtypes = [P, C.c_int]
         for fn in ("rb_bbox", "rb_build", "rb_summarize", "rb_sort", "rb_force",
                    "rb_integrate", "rb_step", "rb_tree"):
             getattr(L, fn).argtypes = [P]
@@ -123,6 +124,12 @@ class Oracle:
             t = np.ascontiguousarray(theta, dtype=np.float32)
             assert t.shape == (self.n,)
             lib().rb_set_theta_body(self._p, t.ctypes.data)
+
+    def enable_ebound(self, on=True):
+        lib().rb_enable_ebound(self._p, int(bool(on)))
+
+    def ebound(self):
+        return _arr(self.s.ebound, self.n, np.float32)
 
     def _call(self, fn):
         return getattr(lib(), fn)(self._p)

@@ -84,6 +84,7 @@ void rb_destroy(rb_sim* s) {
     free(s->kx); free(s->ky); free(s->kz);
     free(s->kvx); free(s->kvy); free(s->kvz);
     free(s->theta_body);
+    free(s->ebound);
     free(s->child); free(s->count); free(s->start); free(s->sorted);
     free(s);
 }
@@ -111,6 +112,11 @@ void rb_load(rb_sim* s, const float* x, const float* y, const float* z,
     s->maxdepth = 1;
     s->error = 0;
     s->interactions = 0;
+}
+
+void rb_enable_ebound(rb_sim* s, int enable) {
+    if (enable && !s->ebound) s->ebound = (float*)calloc(s->n, sizeof(float));
+    if (!enable) { free(s->ebound); s->ebound = NULL; }
 }
 
 void rb_set_theta_body(rb_sim* s, const float* theta) {
@@ -332,13 +338,13 @@ int rb_force(rb_sim* s) {
         const int cnt = hi - lo;
         int bidx[64];
         float px[64], py[64], pz[64], t0[64];
-        float ax[64], ay[64], az[64];
+        float ax[64], ay[64], az[64], eb[64];
         int inter[64];
         for (int k = 0; k < cnt; ++k) {
             int b = s->sorted[lo + k];
             bidx[k] = b;
             px[k] = s->x[b]; py[k] = s->y[b]; pz[k] = s->z[b];
-            ax[k] = ay[k] = az[k] = 0.0f;
+            ax[k] = ay[k] = az[k] = eb[k] = 0.0f;
             inter[k] = 0;
             if (s->theta_body) {
                 float th = s->theta_body[b];
@@ -373,12 +379,15 @@ int rb_force(rb_sim* s) {
                         }
                     }
                     if (ch < n || accept) {
+                        /* full width of a child of a level-`depth` cell: r * 2^-depth */
+                        const float s2 = ch >= n ? ldexpf(rr, -2 * depth) : 0.0f;
                         for (int k = 0; k < cnt; ++k) {
                             float rd = 1.0f / sqrtf(d2s[k]);
                             float f = cmn * rd * rd * rd;
                             ax[k] = madd(fma, dxs[k], f, ax[k]);
                             ay[k] = madd(fma, dys[k], f, ay[k]);
                             az[k] = madd(fma, dzs[k], f, az[k]);
+                            eb[k] += f * rd * s2;
                             inter[k]++;
                         }
                     } else {
@@ -413,6 +422,7 @@ int rb_force(rb_sim* s) {
             s->ax[b] = gx;
             s->ay[b] = gy;
             s->az[b] = gz;
+            if (s->ebound) s->ebound[b] = eb[k] * s->G;
             total += inter[k];
         }
     }

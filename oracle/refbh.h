@@ -33,6 +33,7 @@ typedef struct rb_sim {
     float *vx, *vy, *vz, *ax, *ay, *az;   /* [n] */
     float *kx, *ky, *kz, *kvx, *kvy, *kvz; /* [n] Kahan compensation (precise mode) */
     float *theta_body;              /* [n] optional per-body theta (NULL: fixed) */
+    float *ebound;                  /* [n] optional: sum over accepted cells of m s^2 / d^4 */
     int *child;                     /* [8*(nn+1)] */
     int *count, *start;             /* [nn+1] */
     int *sorted;                    /* [n] */
@@ -49,6 +50,7 @@ void rb_destroy(rb_sim* s);
 void rb_load(rb_sim* s, const float* x, const float* y, const float* z,
              const float* vx, const float* vy, const float* vz, const float* m);
 void rb_set_theta_body(rb_sim* s, const float* theta);   /* NULL: fixed theta */
+void rb_enable_ebound(rb_sim* s, int enable);   /* accumulate the quadrupole error bound */
 
 int rb_bbox(rb_sim* s);
 int rb_build(rb_sim* s);

@@ -1,0 +1,140 @@
+"""Learned per-body opening angle: training kernels against the FP64 CPU reference, the
+device features against a recomputation from the tree, the BF16 tensor-core inference
+against a BF16-emulating reference, the per-body-angle walk against the oracle, and the
+gain of the trained model over the fixed angle."""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from helpers import acc_rel, gpu_sim, oracle_for, plummer
+
+pytestmark = pytest.mark.gpu
+
+
+def _lib():
+    from nbh import _lib as L
+    return L, L.load()
+
+
+def test_mlp_gradient_matches_fp64_reference():
+    import mlp_ref
+    L, lib = _lib()
+    rng = np.random.default_rng(0)
+    n = 3000
+    p = (rng.standard_normal(mlp_ref.NPARAMS) * 0.3).astype(np.float32)
+    X = rng.standard_normal((n, 12)).astype(np.float32)
+    T = rng.standard_normal(n).astype(np.float32)
+    g = np.empty(mlp_ref.NPARAMS, np.float32)
+    loss = C.c_float()
+    L.check(lib.nbh_mlp_grad(0, p.ctypes.data, X.ctypes.data, T.ctypes.data, n, 0.2, g.ctypes.data, C.byref(loss)))
+    rl, rg = mlp_ref.grad(p, X, T, 0.2)
+    assert abs(loss.value - rl) <= 1e-5 * max(1.0, abs(rl))
+    # FP32 sums of 3000 terms against FP64: relative to the gradient's scale
+    scale = np.abs(rg).max()
+    assert np.abs(g - rg).max() <= 2e-5 * scale, np.abs(g - rg).max() / scale
+    y = np.empty(n, np.float32)
+    L.check(lib.nbh_mlp_forward(0, p.ctypes.data, X.ctypes.data, n, y.ctypes.data))
+    np.testing.assert_allclose(y, mlp_ref.forward(p, X), rtol=1e-4, atol=1e-4)
+
+
+def test_mlp_training_fits_quantile():
+    from nbh import learned as LR
+    rng = np.random.default_rng(1)
+    n = 20000
+    X = rng.standard_normal((n, 12)).astype(np.float32)
+    Y = (0.3 * X[:, 0] - 0.2 * X[:, 3] + 0.1 * rng.standard_normal(n) - 0.5).astype(np.float32)
+    m = LR.train(X, Y, quantile=0.2, iters=800)
+    import mlp_ref
+    pred = mlp_ref.forward(m["params"], (X - m["mean"]) * m["inv_std"])
+    frac_below = (Y < pred).mean()
+    assert 0.1 <= frac_below <= 0.3, frac_below           # ~20% of targets below the prediction
+    assert np.corrcoef(pred, Y)[0, 1] > 0.9
+
+
+def test_features_match_tree_recomputation():
+    import mlp_ref
+    from nbh import learned as LR
+    n = 40000
+    arrs = plummer(n, seed=3)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    g.load(*arrs)
+    g.step(2)
+    th = np.random.default_rng(2).uniform(0.4, 0.9, n).astype(np.float32)
+    ax, ay, az, eb, _ = LR.probe(g, th)
+    F = LR.features(g, use_probe=True)
+    t = g.tree()
+    st = g.read()
+    R = mlp_ref.features_from_tree(t, st["x"], st["y"], st["z"], np.stack([ax, ay, az], 1), eb, th, 0.05)
+    np.testing.assert_allclose(F, R, rtol=2e-4, atol=2e-4)
+
+
+def _model(seed=0):
+    from nbh import learned as LR
+    rng = np.random.default_rng(seed)
+    m = {"params": (LR.init_params(seed) * 0.5).astype(np.float32),
+         "mean": rng.standard_normal(12).astype(np.float32) * 0.1,
+         "inv_std": np.full(12, 0.8, np.float32), "theta_min": 0.3, "theta_max": 1.0}
+    return m
+
+
+def test_bf16_inference_matches_reference():
+    import mlp_ref
+    from nbh import learned as LR
+    n = 50000
+    arrs = plummer(n, seed=4)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    g.load(*arrs)
+    m = _model(3)
+    LR.install(g, m)
+    g.step(2)                                  # fixed angle, then the model
+    F = LR.features(g, use_probe=False)        # what the next step's theta stage sees
+    g.step(1)
+    th = LR.read_theta(g)
+    y = mlp_ref.forward_bf16(m["params"], (F - m["mean"]) * m["inv_std"])
+    ref = np.clip(np.exp(y.astype(np.float64)), 0.3, 1.0)
+    np.testing.assert_allclose(th, ref, rtol=2e-3, atol=1e-4)
+    assert th.min() >= 0.3 - 1e-6 and th.max() <= 1.0 + 1e-6
+
+
+def test_per_body_theta_walk_matches_oracle():
+    from nbh import learned as LR
+    n = 30000
+    arrs = plummer(n, seed=5)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    g.load(*arrs)
+    th = np.random.default_rng(7).uniform(0.35, 0.95, n).astype(np.float32)
+    ax, ay, az, eb, inter = LR.probe(g, th)
+    o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=32, fma=True)
+    o.load(*arrs)
+    o.set_theta_body(th)
+    o.enable_ebound()
+    o.tree()
+    o.force()
+    os_ = o.state()
+    assert inter == o.interactions
+    rel, _ = acc_rel({"ax": ax, "ay": ay, "az": az}, os_)
+    assert rel.max() <= 1e-4 and np.median(rel) <= 2e-6
+    np.testing.assert_allclose(eb, o.ebound(), rtol=1e-4, atol=1e-12)
+
+
+MODEL = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gpu-nbody_gb300", "nbh",
+                     "models", "theta_plummer.npz")
+
+
+@pytest.mark.skipif(not os.path.exists(MODEL), reason="trained model not present")
+def test_trained_model_gains_over_fixed_theta():
+    """The committed model on a Plummer sphere it was not trained on: fewer interactions
+    than theta = 0.5 at an equal or lower p99 force error against FP64 (4096 bodies)."""
+    import sys
+    from nbh import learned as LR
+    from nbh import train_theta as TT
+    from nbh import universe as U
+    n = 1 << 20
+    arrs = U.PlummerUniverseGenerator(seed=404).arrays(n)
+    r = TT.evaluate(arrs, LR.load_model(MODEL))
+    gain = r["plain"]["interactions"] / r["learned"]["interactions"]
+    print("learned-theta gain %.3fx, p99 %.3e vs %.3e" % (gain, r["learned"]["p99"], r["plain"]["p99"]), file=sys.stderr)
+    assert gain > 1.05
+    assert r["learned"]["p99"] <= 1.05 * r["plain"]["p99"]
