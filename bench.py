@@ -38,6 +38,9 @@ for _p in (os.path.join(ROOT, "gpu-nbody_gb300"), os.path.join(ROOT, "oracle")):
 METRIC = "ms/step at 1M bodies, plain vs learned-theta at equal p99 force error; Gint/s"
 FLOPS_PER_INTERACTION = 20          # 3 sub, 3 fma (d^2+eps^2), rsqrt, 3 mul, 3 fma, ~7 more
 HBM_FALLBACK_GBS = 6800.0
+# DRAM bytes (read + write) of one force launch on the 1,048,576-body Plummer workload,
+# from the ncu capture summarised in profiles/force_kernel_plummer1M.md.
+FORCE_TRAFFIC_BYTES_1M = 182_850_048 + 22_608_640
 
 # Algorithmic bytes per body / per cell of the memory-bound stages (minimum traffic:
 # every byte read and written once).
@@ -177,6 +180,36 @@ def _config(args):
             "l2": "flushed before every timed step (256 MiB write)", "parallelism": "replicas"}
 
 
+def _step_error(sim, idx, O, np):
+    """Relative force error of the next step's accelerations against the FP64 direct sum
+    at the positions that step starts from (sampled bodies)."""
+    ref = sim.direct_f64(idx)
+    sim.step(1)
+    st = sim.read()
+    e = O.rel_force_error(st["ax"][idx], st["ay"][idx], st["az"][idx], *ref)
+    return {"median": float(np.median(e)), "p99": float(np.percentile(e, 99)), "samples": int(idx.size),
+            "vs": "FP64 direct sum", "interactions": int(sim.stats()["interactions"])}
+
+
+def _timed_steps(sim, steps, flush_l2, stream, torch, dev):
+    """Device time of `steps` single-step graph launches, L2 flushed before each."""
+    torch.cuda.synchronize(dev)
+    evs = []
+    for _ in range(steps):
+        flush_l2(stream)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.step_async(1)
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize(dev)
+    st = sim.stats()
+    if st["status"] != 0:
+        raise RuntimeError("device status %d during the timed steps" % st["status"])
+    return [a.elapsed_time(b) for a, b in evs], st
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -189,6 +222,7 @@ def main():
     ap.add_argument("--dt", type=float, default=0.01)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--error-samples", type=int, default=4096)
     ap.add_argument("--profile-only", action="store_true",
                     help="load, warm up and run the timed steps only (for ncu captures)")
@@ -203,6 +237,7 @@ def main():
 
     import nbh
     import oracle as O
+    from nbh import learned as LR
 
     rank, world, local = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1), _env_int("LOCAL_RANK", 0)
     dist = None
@@ -215,62 +250,39 @@ def main():
 
     arrs = workload(args.n, args.seed + rank)
     n = args.n
-    sim = nbh.Simulation(theta=args.theta, eps=args.eps, dt=args.dt, device=local)
-    sim.load(*arrs)
-
-    # force error of the first step against the FP64 direct sum on sampled bodies
-    force_error = None
-    if not args.profile_only:
-        rng = np.random.default_rng(17)
-        idx = rng.choice(n, min(args.error_samples, n), replace=False).astype(np.int32)
-        ref = sim.direct_f64(idx)
-        sim.step(1)
-        st0 = sim.read()
-        err = O.rel_force_error(st0["ax"][idx], st0["ay"][idx], st0["az"][idx], *ref)
-        force_error = {"median": float(np.median(err)), "p99": float(np.percentile(err, 99)),
-                       "samples": int(idx.size), "vs": "FP64 direct sum"}
-
-    stream = torch.cuda.ExternalStream(sim.stream, device=dev)
+    idx = np.sort(np.random.default_rng(17).choice(n, min(args.error_samples, n), replace=False)).astype(np.int32)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    def flush_l2():
+    def flush_l2(stream):
         with torch.cuda.stream(stream):
             flush.zero_()
 
-    for _ in range(args.warmup):
-        flush_l2()
-        sim.step(1)
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
 
+    # ---- plain fixed theta: warm-up, error of one step, timed steps ---------------------
+    sim = nbh.Simulation(theta=args.theta, eps=args.eps, dt=args.dt, device=local)
+    sim.load(*arrs)
+    stream = torch.cuda.ExternalStream(sim.stream, device=dev)
+    for _ in range(args.warmup):
+        flush_l2(stream)
+        sim.step(1)
+    force_error = None if args.profile_only else _step_error(sim, idx, O, np)
     clocks = ClockSampler(local) if rank == 0 else None
     if clocks:
         clocks.start()
     if dist:
         dist.barrier()
-    torch.cuda.synchronize(dev)
-    evs = []
-    for _ in range(args.steps):
-        flush_l2()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        sim.step_async(1)
-        e1.record(stream)
-        evs.append((e0, e1))
-    torch.cuda.synchronize(dev)
+    step_ms, st = _timed_steps(sim, args.steps, flush_l2, stream, torch, dev)
     if dist:
         dist.barrier()
     clock_info = clocks.stop() if clocks else None
-    st = sim.stats()
-    if st["status"] != 0:
-        raise RuntimeError("device status %d during the timed steps" % st["status"])
-    step_ms = [a.elapsed_time(b) for a, b in evs]
-    ms = sum(step_ms) / len(step_ms)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(step_ms) / len(step_ms))
     interactions = int(st["interactions"])
-
     if args.profile_only:
         if rank == 0:
             print(json.dumps({"profile_only": True, "ms_per_step": ms, "interactions": interactions}))
@@ -309,7 +321,10 @@ def main():
     achieved = FLOPS_PER_INTERACTION * inter_ts / (force_ms * 1e-3) / 1e12
     roofline = {"bound": "fp32", "kernel": "force_kernel<32,FMA>", "achieved": achieved,
                 "peak": fp32.value, "unit": "TFLOP/s", "frac": achieved / fp32.value,
-                "traffic": None, "flops_per_interaction": FLOPS_PER_INTERACTION,
+                "traffic": FORCE_TRAFFIC_BYTES_1M if n == 1 << 20 else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
+                                  "(profiles/force_kernel_plummer1M.md)",
+                "flops_per_interaction": FLOPS_PER_INTERACTION,
                 "peak_source": "measured FP32 FMA loop on this GPU (nbh_measure_fp32_peak); "
                                "MEASURED_PEAKS.json holds only HBM and bf16 peaks",
                 "hbm_peak_GBps": hbm_peak, "hbm_peak_source": peak_src}
@@ -341,6 +356,35 @@ def main():
         t = torch.tensor([e2e_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
+
+    # ---- learned per-body theta: same protocol ----------------------------------------
+    learned = None
+    model_path = LR.default_model_path()
+    if not args.no_learned and os.path.exists(model_path):
+        model = LR.load_model(model_path)
+        ls = nbh.Simulation(theta=args.theta, eps=args.eps, dt=args.dt, device=local)
+        ls.load(*arrs)
+        LR.install(ls, model)
+        lstream = torch.cuda.ExternalStream(ls.stream, device=dev)
+        for _ in range(args.warmup):
+            flush_l2(lstream)
+            ls.step(1)
+        lerr = _step_error(ls, idx, O, np)
+        lstep_ms, lst = _timed_steps(ls, args.steps, flush_l2, lstream, torch, dev)
+        lms = max_over_ranks(sum(lstep_ms) / len(lstep_ms))
+        th = LR.read_theta(ls)
+        learned = {
+            "ms_per_step": lms / world, "speedup_vs_plain": ms / lms,
+            "force_error": lerr, "p99_vs_plain": lerr["p99"] / force_error["p99"],
+            "equal_or_lower_p99": bool(lerr["p99"] <= force_error["p99"]),
+            "interactions_per_step": int(lst["interactions"]),
+            "interaction_ratio_vs_plain": interactions / max(1, int(lst["interactions"])),
+            "theta_mean": float(th.mean()), "theta_p10": float(np.percentile(th, 10)),
+            "theta_p90": float(np.percentile(th, 90)),
+            "model": os.path.relpath(model_path, ROOT),
+            "gint_per_s": int(lst["interactions"]) * world / (lms * 1e-3) / 1e9,
+        }
+        ls.close()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -374,6 +418,7 @@ def main():
             "gpu_launches": 6 * args.steps,
             "clocks": clock_info,
             "cpu_baseline": cpu,
+            "learned_theta": learned,
         }
         print(json.dumps(line))
     sim.close()

@@ -718,6 +718,28 @@ int nbh_direct_f64(nbh_sim* sim, int32_t nidx, const int32_t* idx, double* ax, d
     return NBH_OK;
 }
 
+int nbh_selftest_wait(int32_t device, int64_t limit_ns, int32_t* status) {
+    nbh_sim* sim = nullptr;
+    if (!status || limit_ns <= 0 || limit_ns > 10000000000LL) return fail(nullptr, NBH_ERR_INVALID, "bad arguments");
+    CK(cudaSetDevice(device));
+    int* flag = nullptr;
+    DevState* st = nullptr;
+    CK(cudaMalloc(reinterpret_cast<void**>(&flag), sizeof(int)));
+    CK(cudaMalloc(reinterpret_cast<void**>(&st), sizeof(DevState)));
+    const int lock = kLock;
+    CK(cudaMemcpy(flag, &lock, sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemset(st, 0, sizeof(DevState)));
+    launch_wait_selftest(flag, (unsigned long long)limit_ns, st, nullptr);
+    cudaError_t e = cudaDeviceSynchronize();
+    DevState h{};
+    if (e == cudaSuccess) e = cudaMemcpy(&h, st, sizeof(DevState), cudaMemcpyDeviceToHost);
+    cudaFree(flag);
+    cudaFree(st);
+    if (e != cudaSuccess) return cuda_fail(nullptr, "wait self-test", e);
+    *status = h.status;
+    return NBH_OK;
+}
+
 // ---- learned opening angle -----------------------------------------------------------
 
 int nbh_set_theta_model(nbh_sim* sim, const float* params, int32_t nparams, const float* feat_mean,

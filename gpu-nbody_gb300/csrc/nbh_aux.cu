@@ -204,4 +204,15 @@ void launch_direct_f64(const float4* node4, int nidx, const int* idx, const int2
     direct_f64_kernel<<<grid, kDirectTile, 0, s>>>(node4, nidx, idx, range, eps2, G, out);
 }
 
+// Self-test of the bounded wait: waits on a flag that nothing changes and must come back
+// with NBH_ERR_TIMEOUT in the status word (no fault, no hang), after which the context is
+// still usable.
+__global__ void wait_selftest_kernel(const int* flag, unsigned long long limit_ns, DevState* st) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) bounded_wait_ne(flag, kLock, limit_ns, st, 256, nullptr);
+}
+
+void launch_wait_selftest(const int* flag, unsigned long long limit_ns, DevState* st, cudaStream_t s) {
+    wait_selftest_kernel<<<1, 32, 0, s>>>(flag, limit_ns, st);
+}
+
 }  // namespace nbh

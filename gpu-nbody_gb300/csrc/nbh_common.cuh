@@ -144,6 +144,27 @@ __device__ __forceinline__ int cas_acquire(int* p, int cmp, int val) {
 // L2 (cache-global) vector load: bypasses L1, so a line another SM just wrote is current.
 __device__ __forceinline__ float4 ld_cg4(const float4* p) { return __ldcg(p); }
 
+// Bounded wait until *p != value: polls from L2 with exponential back-off (min_ns doubling
+// to kBackoffMaxNs) and gives up after limit_ns, raising NBH_ERR_TIMEOUT, or as soon as
+// another stage raised an error.  Returns the value seen, or `value` when it gave up.
+__device__ __forceinline__ int bounded_wait_ne(const int* p, int value, unsigned long long limit_ns, DevState* st,
+                                               unsigned min_ns, int* polls) {
+    const unsigned long long t0 = global_ns();
+    unsigned backoff = min_ns;
+    for (;;) {
+        const int v = ld_relaxed(p);
+        if (v != value) return v;
+        if (load_status(st)) return value;
+        if (global_ns() - t0 > limit_ns) {
+            raise_error(st, NBH_ERR_TIMEOUT);
+            return value;
+        }
+        if (polls) ++*polls;
+        __nanosleep(backoff);
+        backoff = backoff * 2 < kBackoffMaxNs ? backoff * 2 : kBackoffMaxNs;
+    }
+}
+
 // Order-preserving float <-> uint mapping for atomicMin/atomicMax on extents.
 __device__ __forceinline__ unsigned f2ord(float f) {
     unsigned u = __float_as_uint(f);

@@ -23,6 +23,8 @@ void launch_export4(int n, const float4* node4, const float4* vel, float4* pos4,
 void launch_direct_f64(const float4* node4, int nidx, const int* idx, const int2* range, double eps2, double G,
                        double* out, int ysplit, cudaStream_t s);
 
+struct DevState;
+void launch_wait_selftest(const int* flag, unsigned long long limit_ns, DevState* st, cudaStream_t s);
 void launch_fma_peak(float* sink, int iters, int grid, int block, cudaStream_t s);
 
 int occupancy_sort(int* blocks_per_sm);

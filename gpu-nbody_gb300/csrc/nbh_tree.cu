@@ -145,8 +145,6 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
             float cx = rc.x, cy = rc.y, cz = rc.z;
             int path = octant(cx, cy, cz, bp.x, bp.y, bp.z);
             int* slot = cell_child(p, node) + path;
-            unsigned long long t0 = 0;
-            unsigned backoff = kBackoffMinNs;
             // Slots are read through L1.  A slot that holds a cell index keeps it for the
             // rest of the build, and each cell's slots are one 32-byte sector first read
             // after the cell was published, so a cell index read from L1 is always right;
@@ -233,20 +231,11 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
                     ch = seen;
                     continue;
                 }
-                // the slot is locked by a split in progress: wait (bounded), re-read from L2
-                if (load_status(p.st)) goto finish;
-                const unsigned long long now = global_ns();
-                if (t0 == 0) t0 = now;
-                else if (now - t0 > kWaitNs) {
-                    raise_error(p.st, NBH_ERR_TIMEOUT);
-                    goto finish;
-                }
-                // back off exponentially: thousands of descents may wait on the same few
-                // slots near the root early in the build
-                ++waits;
-                __nanosleep(backoff);
-                backoff = min(backoff * 2, kBackoffMaxNs);
-                ch = ld_relaxed(slot);
+                // the slot is locked by a split in progress: wait (bounded, backed off:
+                // thousands of descents may wait on the same few slots near the root early
+                // in the build) until it holds the new subtree
+                ch = bounded_wait_ne(slot, kLock, kWaitNs, p.st, kBackoffMinNs, &waits);
+                if (ch == kLock) goto finish;
             }
         }
     }

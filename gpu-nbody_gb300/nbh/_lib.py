@@ -80,6 +80,7 @@ SIGNATURES = {
     "nbh_export_float4": (C.c_int, [_P, _P, _P]),
     "nbh_last_error_message": (C.c_char_p, [_P]),
     "nbh_get_stream": (C.c_void_p, [_P]),
+    "nbh_selftest_wait": (C.c_int, [C.c_int32, C.c_int64, _I]),
     "nbh_measure_fp32_peak": (C.c_int, [C.c_int32, _D]),
     "nbh_last_error": (C.c_int, [_P]),
     "nbh_number_of_nodes": (C.c_int32, [C.c_int32, C.c_float]),

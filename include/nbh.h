@@ -167,6 +167,11 @@ void* nbh_get_stream(nbh_sim* sim);
  * roofline denominator of the force traversal, which runs on the FP32 pipes. */
 int nbh_measure_fp32_peak(int32_t device, double* tflops);
 
+/* Failure-detection self-test: one device thread waits, with the same bounded wait the build
+ * uses, on a flag that nothing changes; it must give up after limit_ns and leave
+ * NBH_ERR_TIMEOUT in *status, with the context still usable. */
+int nbh_selftest_wait(int32_t device, int64_t limit_ns, int32_t* status);
+
 /* Last error text of this sim (or of the last failed nbh_create when sim is NULL). */
 const char* nbh_last_error_message(nbh_sim* sim);
 int nbh_last_error(nbh_sim* sim);
