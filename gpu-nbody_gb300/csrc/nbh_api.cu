@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -294,6 +295,108 @@ int alloc_for(nbh_sim* sim, int nbody, int nuniv, int nnodes, int nchunks, int n
 
 }  // namespace
 
+// ---- FP64 direct sum with library-owned scratch (nbh_direct_f64_static) -------------------
+// Some callers cannot allocate device memory while they run: an application whose device
+// memory is handed out up front by its own pool or a fixed budget, or a time-critical loop in
+// which cudaMalloc/cudaFree would synchronise the device and stall other streams.  For them
+// the FP64 direct sum has a variant whose scratch (target indices and three FP64 accumulator
+// columns) lives in this file-scope device array instead of per-call allocations.  The array
+// takes kStaticDirectMax targets (~1.8 MB) on every GPU that loads the library, until exit.
+constexpr int kStaticDirectMax = 65536;
+struct StaticDirectScratch {
+    int idx[kStaticDirectMax];
+    double ax[kStaticDirectMax];
+    double ay[kStaticDirectMax];
+    double az[kStaticDirectMax];
+};
+static __device__ __align__(256) StaticDirectScratch g_direct_scratch;
+
+// Device address of g_direct_scratch, per device.  In host code the symbol's name is only a
+// host-side stand-in, so the address is taken once per device with cudaGetSymbolAddress, with
+// that device current.
+constexpr int kMaxDevices = 64;
+static StaticDirectScratch* g_direct_scratch_ptr[kMaxDevices] = {};
+static std::mutex g_direct_scratch_mu;
+
+static cudaError_t direct_scratch_for(int device, StaticDirectScratch** out) {
+    std::lock_guard<std::mutex> lk(g_direct_scratch_mu);
+    if (!g_direct_scratch_ptr[device]) {
+        void* ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_direct_scratch);
+        if (e != cudaSuccess) return e;
+        g_direct_scratch_ptr[device] = static_cast<StaticDirectScratch*>(ptr);
+    }
+    *out = g_direct_scratch_ptr[device];
+    return cudaSuccess;
+}
+
+// Same sum as direct_f64_kernel; each target finds its universe's body range from the
+// universe offsets itself, and the partial sums land in the scratch's SoA columns.
+__global__ void __launch_bounds__(256) direct_f64_static_kernel(const float4* __restrict__ node4,
+                                                                const int* __restrict__ ubody, int nuniv,
+                                                                StaticDirectScratch* sc, int nidx, double eps2,
+                                                                double G) {
+    __shared__ double tile[256][4];
+    __shared__ int blo, bhi;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = t < nidx;
+    int i = 0, lo = 0, hi = 0;
+    if (valid) {
+        i = sc->idx[t];
+        int a = 0, b = nuniv;          // last universe whose first body is <= i
+        while (b - a > 1) {
+            const int mid = (a + b) >> 1;
+            if (ubody[mid] <= i) a = mid;
+            else b = mid;
+        }
+        lo = ubody[a];
+        hi = ubody[a + 1];
+    }
+    if (threadIdx.x == 0) { blo = 0x7fffffff; bhi = 0; }
+    __syncthreads();
+    if (valid) { atomicMin(&blo, lo); atomicMax(&bhi, hi); }
+    __syncthreads();
+    const int l0 = blo, h0 = bhi;
+    if (l0 >= h0) return;
+    const int per = (h0 - l0 + gridDim.y - 1) / gridDim.y;
+    const int s0 = l0 + blockIdx.y * per, s1 = min(h0, s0 + per);
+    double xi = 0, yi = 0, zi = 0;
+    if (valid) {
+        const float4 q = node4[i];
+        xi = q.x; yi = q.y; zi = q.z;
+    }
+    double sx = 0, sy = 0, sz = 0;
+    for (int base = s0; base < s1; base += 256) {
+        const int j = base + threadIdx.x;
+        __syncthreads();
+        if (j < s1) {
+            const float4 q = node4[j];
+            tile[threadIdx.x][0] = q.x; tile[threadIdx.x][1] = q.y;
+            tile[threadIdx.x][2] = q.z; tile[threadIdx.x][3] = q.w;
+        }
+        __syncthreads();
+        const int cnt = min(256, s1 - base);
+        if (valid) {
+            for (int k = 0; k < cnt; ++k) {
+                const int jj = base + k;
+                if (jj < lo || jj >= hi) continue;
+                const double dx = tile[k][0] - xi, dy = tile[k][1] - yi, dz = tile[k][2] - zi;
+                const double d2 = dx * dx + dy * dy + dz * dz + eps2;
+                const double inv = 1.0 / sqrt(d2);
+                const double f = tile[k][3] * inv * inv * inv;
+                sx += dx * f;
+                sy += dy * f;
+                sz += dz * f;
+            }
+        }
+    }
+    if (valid) {
+        atomicAdd(&sc->ax[t], G * sx);
+        atomicAdd(&sc->ay[t], G * sy);
+        atomicAdd(&sc->az[t], G * sz);
+    }
+}
+
 extern "C" {
 
 void nbh_config_default(nbh_config* cfg) {
@@ -347,6 +450,7 @@ int nbh_create(const nbh_config* cfg_in, nbh_sim** out) {
     if (prop.major * 10 + prop.minor < 100)
         return fail(nullptr, NBH_ERR_NODEVICE, "device is not a Blackwell-class GPU (built for sm_103a)");
     nbh_sim* sim = new nbh_sim();
+    sim->err.reserve(1024);   // error messages of later calls then fit without allocating
     sim->cfg = cfg;
     sim->device = cfg.device;
     sim->sms = prop.multiProcessorCount;
@@ -715,6 +819,41 @@ int nbh_direct_f64(nbh_sim* sim, int32_t nidx, const int32_t* idx, double* ax, d
         ay[t] = out[3 * t + 1];
         az[t] = out[3 * t + 2];
     }
+    return NBH_OK;
+}
+
+int nbh_direct_f64_static(nbh_sim* sim, int32_t nidx, const int32_t* idx, double* ax, double* ay, double* az) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_direct_f64_static before nbh_load");
+    if (nidx < 0 || (nidx > 0 && (!idx || !ax || !ay || !az))) return fail(sim, NBH_ERR_INVALID, "bad arguments");
+    if (nidx > kStaticDirectMax)
+        return fail(sim, NBH_ERR_INVALID,
+                    "nbh_direct_f64_static takes at most 65536 bodies per call (its scratch is a fixed "
+                    "device array); split the list or use nbh_direct_f64");
+    if (nidx == 0) return NBH_OK;
+    for (int t = 0; t < nidx; ++t)
+        if (idx[t] < 0 || idx[t] >= sim->nbody) return fail(sim, NBH_ERR_INVALID, "body index out of range");
+    CK(cudaSetDevice(sim->device));
+    if (sim->device < 0 || sim->device >= kMaxDevices) return fail(sim, NBH_ERR_INVALID, "device ordinal too large");
+    StaticDirectScratch* sc = nullptr;
+    CK(direct_scratch_for(sim->device, &sc));
+    cudaStream_t s = sim->stream;
+    // The scratch keeps the previous call's contents: the accumulators must start at zero.
+    CK(cudaMemsetAsync(sc->ax, 0, sizeof(double) * nidx, s));
+    CK(cudaMemsetAsync(sc->ay, 0, sizeof(double) * nidx, s));
+    CK(cudaMemsetAsync(sc->az, 0, sizeof(double) * nidx, s));
+    CK(cudaMemcpyAsync(sc->idx, idx, sizeof(int) * nidx, cudaMemcpyHostToDevice, s));
+    const nbh_config& c = sim->cfg;
+    const float eps2f = c.eps2 > 0.0f ? c.eps2 : c.eps * c.eps;
+    const int bx = (nidx + 255) / 256;
+    const int ysplit = std::max(1, std::min(256, (8 * sim->sms + bx - 1) / bx));
+    direct_f64_static_kernel<<<dim3(bx, ysplit), 256, 0, s>>>(sim->node4, sim->ubody, sim->nuniv, sc, nidx,
+                                                              (double)eps2f, (double)c.G);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ax, sc->ax, sizeof(double) * nidx, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ay, sc->ay, sizeof(double) * nidx, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(az, sc->az, sizeof(double) * nidx, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
     return NBH_OK;
 }
 

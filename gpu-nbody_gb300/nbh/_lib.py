@@ -27,6 +27,7 @@ NBH_ARITH_FMA = 0
 NBH_ARITH_REFERENCE = 1
 NBH_MLP_PARAMS = 4993
 NBH_MLP_FEATURES = 12
+NBH_DIRECT_STATIC_MAX = 65536
 
 ERROR_NAMES = {
     NBH_OK: "NBH_OK", NBH_ERR_INVALID: "NBH_ERR_INVALID", NBH_ERR_CUDA: "NBH_ERR_CUDA",
@@ -86,6 +87,7 @@ SIGNATURES = {
     "nbh_number_of_nodes": (C.c_int32, [C.c_int32, C.c_float]),
     "nbh_read_tree": (C.c_int, [_P] + [_P] * 8),
     "nbh_direct_f64": (C.c_int, [_P, C.c_int32, _P, _P, _P, _P]),
+    "nbh_direct_f64_static": (C.c_int, [_P, C.c_int32, _P, _P, _P, _P]),
     "nbh_generate_uniform_ball": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_float, C.c_float] + [_P] * 7),
     "nbh_generate_plummer": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_float, C.c_float] + [_P] * 7),
     "nbh_generate_disc": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_float,

@@ -245,6 +245,21 @@ int nbh_mlp_grad(int32_t device, const float* params, const float* X, const floa
                  float quantile, float* grad, float* loss);
 int nbh_mlp_forward(int32_t device, const float* params, const float* X, int32_t n, float* y);
 
+/* Same FP64 direct sum as nbh_direct_f64, for callers that cannot allocate device memory
+ * while they run (an application whose device memory is handed out up front by its own pool
+ * or budget, or a time-critical loop in which cudaMalloc/cudaFree would synchronise the
+ * device).  It makes no device or host allocation: its scratch (the index list and three
+ * FP64 accumulator columns) is a fixed array inside the library, holding at most
+ * NBH_DIRECT_STATIC_MAX bodies per call; larger lists are rejected with NBH_ERR_INVALID.
+ * That array is reserved on every GPU that loads the library until the process exits.  The
+ * first call on a device looks the array's device address up (cudaGetSymbolAddress, with the
+ * sim's device current), so make that first call before any stream capture.  All calls share
+ * the array: it is cleared at the start of every call, and calls that overlap on the GPU (two
+ * sims on different streams at the same time) race on it.  No counterpart in the reference. */
+#define NBH_DIRECT_STATIC_MAX 65536
+int nbh_direct_f64_static(nbh_sim* sim, int32_t nidx, const int32_t* idx,
+                          double* ax, double* ay, double* az);
+
 /* ---- Seeded universe generators (UniverseGenerator implementations) ------------------ */
 /* All fill caller arrays of n floats at offset `offset`, deterministic in `seed`.
  * Velocity pointers may be NULL where a generator leaves velocities unset. */
