@@ -36,6 +36,7 @@ for _p in (os.path.join(ROOT, "gpu-nbody_gb300"), os.path.join(ROOT, "oracle")):
         sys.path.insert(0, _p)
 
 METRIC = "ms/step at 1M bodies, plain vs learned-theta at equal p99 force error; Gint/s"
+DEFAULT_VOTE = 64                   # libnbh's default vote width (nbh_config_default)
 FLOPS_PER_INTERACTION = 20          # 3 sub, 3 fma (d^2+eps^2), rsqrt, 3 mul, 3 fma, ~7 more
 HBM_FALLBACK_GBS = 6800.0
 # DRAM bytes (read + write) of one force launch on the 1,048,576-body Plummer workload,
@@ -119,54 +120,102 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def workload(n, seed):
+# Workloads (seeded synthetic inputs of the shapes the benchmark cases name).  "plummer"
+# is the headline; the others are the remaining cases of the same step, measured with
+# the same protocol.
+WORKLOADS = {
+    "plummer": {"n": 1 << 20, "dt": 0.01, "precise": False,
+                "what": "Plummer sphere a=1 M=1, equal masses, DF velocities"},
+    "ball": {"n": 16384, "dt": 0.025, "precise": False,
+             "what": "uniform unit ball, equal masses 1/N, Gaussian velocities sigma 0.05"},
+    "disc": {"n": 1 << 22, "dt": 0.01, "precise": True,
+             "what": "exponential disc rd=1 zd=0.1 (near-circular velocities) + central mass 0.1 "
+                     "+ 10% Plummer halo; Kahan-compensated updates, FP64 extent/root COM"},
+    "ensemble": {"n": 256, "dt": 0.01, "precise": False,
+                 "what": "256 independent Plummer spheres, N per universe log-uniform in "
+                         "[1024, 65536], all advanced in one graph per step"},
+}
+
+
+def ensemble_counts(nuniv, seed, lo=1024, hi=65536):
+    import numpy as np
+    r = np.random.default_rng(seed)
+    return np.exp(r.uniform(np.log(lo), np.log(hi), nuniv)).astype(np.int64).astype(np.int32)
+
+
+def workload(args, seed):
+    """(arrays x y z vx vy vz m, per-universe counts or None)."""
+    import numpy as np
     from nbh import universe as U
-    return U.PlummerUniverseGenerator(seed=seed, a=1.0, M=1.0).arrays(n)
+    if args.workload == "plummer":
+        return U.PlummerUniverseGenerator(seed=seed, a=1.0, M=1.0).arrays(args.n), None
+    if args.workload == "ball":
+        return U.UniformBallUniverseGenerator(seed=seed, radius=1.0, vsigma=0.05).arrays(args.n), None
+    if args.workload == "disc":
+        return U.DiscGalaxyGenerator(seed=seed, rd=1.0, zd=0.1, center_mass=0.1,
+                                     halo_frac=0.1).arrays(args.n), None
+    counts = ensemble_counts(args.n, seed)
+    parts = [U.PlummerUniverseGenerator(seed=seed * 1000 + u, a=1.0, M=1.0).arrays(int(c))
+             for u, c in enumerate(counts)]
+    return tuple(np.concatenate([p[k] for p in parts]) for k in range(7)), counts
 
 
-def cpu_step_time(arrs, args, max_seconds=25.0):
-    """Oracle port (OpenMP, all host threads) on the same workload: seconds per step."""
+def _oracles(arrs, counts, args):
+    """One oracle port instance per universe (the port holds a single universe)."""
     import oracle as O
-    n = arrs[0].size
-    o = O.Oracle(n, theta=args.theta, eps=args.eps, dt=args.dt, vote=32, fma=True)
-    o.load(*arrs)
+    bounds = [0, arrs[0].size] if counts is None else [0] + list(__import__("numpy").cumsum(counts))
+    out = []
+    for a, b in zip(bounds[:-1], bounds[1:]):
+        o = O.Oracle(int(b - a), theta=args.theta, eps=args.eps, dt=args.dt, vote=args.vote_width, fma=True)
+        o.load(*[v[a:b] for v in arrs])
+        out.append(o)
+    return out
+
+
+def cpu_step_time(arrs, counts, args, max_seconds=25.0):
+    """Oracle port (OpenMP, all host threads) on the same workload: seconds per step."""
+    os_ = _oracles(arrs, counts, args)
     t0 = time.perf_counter()
-    o.step()                                   # warm-up (page faults, thread start)
+    for o in os_:
+        o.step()                               # warm-up (page faults, thread start)
     first = time.perf_counter() - t0
     steps = max(1, min(3, int(max_seconds / max(first, 1e-3))))
     t0 = time.perf_counter()
-    o.step(steps)
-    return (time.perf_counter() - t0) / steps, steps, o.interactions
+    for o in os_:
+        o.step(steps)
+    return (time.perf_counter() - t0) / steps, steps, sum(o.interactions for o in os_)
 
 
 def run_reference(args):
     rank = _env_int("RANK", 0)
     if rank != 0:
         return 0
-    arrs = workload(args.n, args.seed)
+    arrs, counts = workload(args, args.seed)
+    args.vote_width = args.vote or DEFAULT_VOTE
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    import oracle as O
-    o = O.Oracle(args.n, theta=args.theta, eps=args.eps, dt=args.dt, vote=32, fma=True)
-    o.load(*arrs)
+    os_ = _oracles(arrs, counts, args)
     for _ in range(args.warmup):
-        o.step()
+        for o in os_:
+            o.step()
     t = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        o.step()
+        for o in os_:
+            o.step()
         t.append(time.perf_counter() - t0)
     ms = 1e3 * sum(t) / len(t)
+    nb = arrs[0].size
     line = {
         "impl": "reference", "metric": METRIC, "value": ms, "unit": "ms/step", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": _config(args),
+        "config": _config(args, nb, counts),
         "cpu_baseline": {"value": ms, "unit": "ms/step", "cores": cores, "kind": "port",
-                         "sample": "%d full steps of the %d-body Plummer workload (oracle/refbh.c, "
-                                   "OpenMP force pass)" % (args.steps, args.n)},
+                         "sample": "%d full steps of the %d-body %s workload (oracle/refbh.c, "
+                                   "OpenMP force pass)" % (args.steps, nb, args.workload)},
         "e2e": {"value": ms, "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "gint_per_s": o.interactions / (ms * 1e-3) / 1e9,
+        "gint_per_s": sum(o.interactions for o in os_) / (ms * 1e-3) / 1e9,
         "note": "the reference's OpenCL kernels need an OpenCL 2.0 runtime and a JVM, absent on "
                 "this box; its CPU restatement (oracle/refbh.c) is timed instead",
     }
@@ -174,10 +223,15 @@ def run_reference(args):
     return 0
 
 
-def _config(args):
-    return {"workload": "plummer-%d" % args.n, "n_bodies": args.n, "distribution": "Plummer a=1 M=1",
-            "theta": args.theta, "eps": args.eps, "dt": args.dt, "G": 1.0, "vote_width": 32,
-            "l2": "flushed before every timed step (256 MiB write)", "parallelism": "replicas"}
+def _config(args, nbodies=None, counts=None):
+    w = WORKLOADS[args.workload]
+    c = {"workload": "%s-%d" % (args.workload, args.n), "n_bodies": nbodies or args.n,
+         "distribution": w["what"], "theta": args.theta, "eps": args.eps, "dt": args.dt, "G": 1.0,
+         "vote_width": args.vote_width, "precise": w["precise"],
+         "l2": "flushed before every timed step (256 MiB write)", "parallelism": "replicas"}
+    if counts is not None:
+        c.update({"universes": len(counts), "min_universe": int(min(counts)), "max_universe": int(max(counts))})
+    return c
 
 
 def _step_error(sim, idx, O, np):
@@ -216,10 +270,13 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="nbh", choices=["nbh", "reference"])
-    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--workload", default="plummer", choices=sorted(WORKLOADS))
+    ap.add_argument("--n", type=int, default=None,
+                    help="bodies (universes for the ensemble); default per workload")
+    ap.add_argument("--vote", type=int, default=None, help="vote width (16, 32, 64; default: the library's)")
     ap.add_argument("--theta", type=float, default=0.5)
     ap.add_argument("--eps", type=float, default=0.05)
-    ap.add_argument("--dt", type=float, default=0.01)
+    ap.add_argument("--dt", type=float, default=None)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
@@ -228,6 +285,11 @@ def main():
                     help="load, warm up and run the timed steps only (for ncu captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    w = WORKLOADS[args.workload]
+    if args.n is None:
+        args.n = w["n"]
+    if args.dt is None:
+        args.dt = w["dt"]
 
     if args.impl == "reference":
         return run_reference(args)
@@ -248,8 +310,18 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    arrs = workload(args.n, args.seed + rank)
-    n = args.n
+    arrs, counts = workload(args, args.seed + rank)
+    n = arrs[0].size
+    precise = WORKLOADS[args.workload]["precise"]
+
+    def new_sim(**kw):
+        s_ = nbh.Simulation(theta=args.theta, eps=args.eps, dt=args.dt, device=local, precise=precise,
+                            vote_width=args.vote, **kw)
+        if counts is None:
+            s_.load(*arrs)
+        else:
+            s_.load_batch(counts, *arrs)
+        return s_
     idx = np.sort(np.random.default_rng(17).choice(n, min(args.error_samples, n), replace=False)).astype(np.int32)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
@@ -265,8 +337,8 @@ def main():
         return float(t.item())
 
     # ---- plain fixed theta: warm-up, error of one step, timed steps ---------------------
-    sim = nbh.Simulation(theta=args.theta, eps=args.eps, dt=args.dt, device=local)
-    sim.load(*arrs)
+    sim = new_sim()
+    args.vote_width = int(sim.config.vote_width)
     stream = torch.cuda.ExternalStream(sim.stream, device=dev)
     for _ in range(args.warmup):
         flush_l2(stream)
@@ -291,8 +363,7 @@ def main():
 
     # per-stage device times (eager launches with events between stages)
     hbm_peak, peak_src = _peaks()
-    ts = nbh.Simulation(theta=args.theta, eps=args.eps, dt=args.dt, device=local, stage_timing=True)
-    ts.load(*arrs)
+    ts = new_sim(stage_timing=True)
     ts.step(2)
     tstream = torch.cuda.ExternalStream(ts.stream, device=dev)
     acc = {k: 0.0 for k in ("ms_bbox", "ms_build", "ms_summarize", "ms_sort", "ms_force", "ms_integrate", "ms_step")}
@@ -319,9 +390,9 @@ def main():
     fp32 = __import__("ctypes").c_double()
     nbh._lib.check(nbh._lib.load().nbh_measure_fp32_peak(local, __import__("ctypes").byref(fp32)))
     achieved = FLOPS_PER_INTERACTION * inter_ts / (force_ms * 1e-3) / 1e12
-    roofline = {"bound": "fp32", "kernel": "force_kernel<32,FMA>", "achieved": achieved,
+    roofline = {"bound": "fp32", "kernel": "force_kernel<%d,FMA>" % args.vote_width, "achieved": achieved,
                 "peak": fp32.value, "unit": "TFLOP/s", "frac": achieved / fp32.value,
-                "traffic": FORCE_TRAFFIC_BYTES_1M if n == 1 << 20 else None,
+                "traffic": FORCE_TRAFFIC_BYTES_1M if (args.workload == "plummer" and n == 1 << 20) else None,
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
                                   "(profiles/force_kernel_plummer1M.md)",
                 "flops_per_interaction": FLOPS_PER_INTERACTION,
@@ -362,8 +433,7 @@ def main():
     model_path = LR.default_model_path()
     if not args.no_learned and os.path.exists(model_path):
         model = LR.load_model(model_path)
-        ls = nbh.Simulation(theta=args.theta, eps=args.eps, dt=args.dt, device=local)
-        ls.load(*arrs)
+        ls = new_sim()
         LR.install(ls, model)
         lstream = torch.cuda.ExternalStream(ls.stream, device=dev)
         for _ in range(args.warmup):
@@ -390,10 +460,11 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-        sec, k, cpu_inter = cpu_step_time(arrs, args)
+        sec, k, cpu_inter = cpu_step_time(arrs, counts, args)
         cpu = {"value": sec * 1e3, "unit": "ms/step", "cores": cores, "kind": "port",
-               "sample": "%d full step(s) of the same %d-body Plummer workload after one warm-up step "
-                         "(oracle/refbh.c, OpenMP force pass; tree stages serial)" % (k, n),
+               "sample": "%d full step(s) of the same %d-body %s workload after one warm-up step "
+                         "(oracle/refbh.c, OpenMP force pass; tree stages serial%s)"
+                         % (k, n, args.workload, "; one port instance per universe" if counts is not None else ""),
                "interactions_per_step": cpu_inter}
 
     if rank == 0:
@@ -401,8 +472,8 @@ def main():
             "metric": METRIC, "value": ms / world, "unit": "ms/step", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic: seeded Plummer sphere (a=1, M=1, DF velocities), %d bodies per replica" % n,
-            "config": _config(args),
+            "data": "synthetic: seeded %s, %d bodies per replica" % (WORKLOADS[args.workload]["what"], n),
+            "config": _config(args, n, counts),
             "gint_per_s": interactions * world / (ms * 1e-3) / 1e9,
             "gint_per_s_force_only": inter_ts / (force_ms * 1e-3) / 1e9,
             "interactions_per_step": interactions,

@@ -45,14 +45,16 @@ struct nbh_sim {
     float* staging = nullptr;      // 10 * nbody floats: x y z vx vy vz ax ay az m
     float* theta_body = nullptr;   // nbody floats when a per-body theta is active
     bool theta_active = false;     // learned opening angle on
+    int theta_every = 1;           // steps between evaluations of the model
+    int theta_group = 0;           // 1: each vote group walks with its smallest angle
     ThetaDev* model = nullptr;     // installed model (device)
     float* model_prm = nullptr;    // its FP32 parameters (device)
     float* probe_theta = nullptr;  // per-body theta of the last force probe (device)
     float* feat = nullptr;         // features of every body (device, nbody * 12)
-    int nchunks = 0, nwarps = 0;
+    int nchunks = 0, nwarps = 0, nitems64 = 0;
     std::vector<int> h_ubody;
     // launch geometry
-    int grid_bbox = 0, grid_build = 0, grid_sum = 0, grid_sort = 0, grid_force = 0, grid_int = 0;
+    int grid_bbox = 0, grid_sum = 0, grid_sort = 0, grid_force = 0, grid_int = 0;
     // graph of one step
     cudaGraphExec_t exec = nullptr;
     // host mirrors
@@ -143,12 +145,15 @@ StepParams step_params(const nbh_sim* sim) {
     p.parent = sim->parent;
     p.sorted = sim->sorted;
     p.theta_body = sim->theta_active ? sim->theta_body : nullptr;
+    p.theta_group = sim->theta_group;
     p.st = sim->st;
     p.ubody = sim->ubody;
     p.ubox = sim->ubox;
     p.uradius = sim->uradius;
     p.chunks = sim->chunks;
     p.warps = sim->warps;
+    p.items64 = sim->warps + sim->nwarps;     // stored after the 32-body items
+    p.nitems64 = sim->nitems64;
     p.nchunks = sim->nchunks;
     p.nwarps = sim->nwarps;
     p.nbody = sim->nbody;
@@ -171,7 +176,7 @@ void enqueue_step(nbh_sim* sim, bool timed) {
     if (timed) cudaEventRecord(sim->ev[0], s);
     launch_bbox(p, sim->grid_bbox, s);
     if (timed) cudaEventRecord(sim->ev[1], s);
-    launch_build(p, sim->grid_build, s);
+    launch_build(p, s);
     launch_link(p, sim->grid_sum, s);
     if (timed) cudaEventRecord(sim->ev[2], s);
     launch_summarize(p, ref, sim->grid_sum, s);
@@ -179,7 +184,15 @@ void enqueue_step(nbh_sim* sim, bool timed) {
     launch_sort(p, sim->grid_sort, s);
     if (sim->theta_active) launch_theta(p, sim->model, sim->theta_body, sim->grid_force, s);
     if (timed) cudaEventRecord(sim->ev[4], s);
-    launch_force(p, sim->cfg.vote_width, ref, sim->theta_active, sim->grid_force, s);
+    if (sim->theta_active && sim->theta_every > 1) {
+        StepParams pg = p;
+        pg.feat_gate = 1;    // the walk before an evaluation records the error bounds
+        launch_force(pg, sim->cfg.vote_width, ref, true, sim->grid_force, s);
+        pg.feat_gate = 2;
+        launch_force(pg, sim->cfg.vote_width, ref, false, sim->grid_force, s);
+    } else {
+        launch_force(p, sim->cfg.vote_width, ref, sim->theta_active, sim->grid_force, s);
+    }
     if (timed) cudaEventRecord(sim->ev[5], s);
     launch_integrate(p, ref, sim->grid_int, s);
     if (timed) cudaEventRecord(sim->ev[6], s);
@@ -191,7 +204,7 @@ void enqueue_tree(nbh_sim* sim, const StepParams& p) {
     const bool ref = sim->cfg.arith == NBH_ARITH_REFERENCE;
     cudaStream_t s = sim->stream;
     launch_bbox(p, sim->grid_bbox, s);
-    launch_build(p, sim->grid_build, s);
+    launch_build(p, s);
     launch_link(p, sim->grid_sum, s);
     launch_summarize(p, ref, sim->grid_sum, s);
     launch_sort(p, sim->grid_sort, s);
@@ -228,8 +241,6 @@ int set_geometry(nbh_sim* sim) {
     CK(static_cast<cudaError_t>(occupancy_force(sim->cfg.vote_width, sim->cfg.arith == NBH_ARITH_REFERENCE,
                                                 &occ_force)));
     sim->grid_bbox = std::max(1, std::min(sim->nchunks, 4 * sms));
-    // one body per thread: a long insertion or climb never delays another body
-    sim->grid_build = std::max(1, sim->nchunks);
     sim->grid_sum = std::max(1, (sim->nbody + 255) / 256);
     sim->grid_sort = std::max(1, std::min(occ_sort * sms, (sim->ncells + 255) / 256));
     sim->grid_force = std::max(1, occ_force * sms);
@@ -409,7 +420,7 @@ void nbh_config_default(nbh_config* cfg) {
     cfg->dt = 0.025f;
     cfg->G = 1.0f;
     cfg->pool_factor = 2.0f;
-    cfg->vote_width = 32;
+    cfg->vote_width = 64;
     cfg->arith = NBH_ARITH_FMA;
     cfg->precise = 0;
     cfg->stage_timing = 0;
@@ -436,8 +447,10 @@ int nbh_create(const nbh_config* cfg_in, nbh_sim** out) {
     if (!(cfg.theta >= 0.0f) || !(cfg.eps > 0.0f || cfg.eps2 > 0.0f) || !std::isfinite(cfg.dt) ||
         !std::isfinite(cfg.G) || !(cfg.pool_factor > 0.0f) || !(cfg.theta2 >= 0.0f) || !(cfg.eps2 >= 0.0f))
         return fail(nullptr, NBH_ERR_INVALID, "theta must be >= 0, eps > 0, dt and G finite, pool_factor > 0");
-    if (cfg.vote_width != 16 && cfg.vote_width != 32)
-        return fail(nullptr, NBH_ERR_INVALID, "vote_width must be 16 or 32");
+    if (cfg.vote_width != 16 && cfg.vote_width != 32 && cfg.vote_width != 64)
+        return fail(nullptr, NBH_ERR_INVALID, "vote_width must be 16, 32 or 64");
+    if (cfg.vote_width == 64 && cfg.arith == NBH_ARITH_REFERENCE)
+        return fail(nullptr, NBH_ERR_INVALID, "vote_width 64 takes FMA arithmetic");
     if (cfg.arith != NBH_ARITH_FMA && cfg.arith != NBH_ARITH_REFERENCE)
         return fail(nullptr, NBH_ERR_INVALID, "arith must be NBH_ARITH_FMA or NBH_ARITH_REFERENCE");
     int ndev = 0;
@@ -522,6 +535,9 @@ int nbh_load_batch(nbh_sim* sim, int32_t nuniv, const int32_t* counts, const flo
         for (int b = lo; b < hi; b += target) chunks.push_back(make_int4(u, b, std::min(hi, b + target), 0));
         for (int s = lo; s < hi; s += 32) warps.push_back(make_int2(s, u));
     }
+    const int nw32 = (int)warps.size();
+    for (int u = 0; u < nuniv; ++u)
+        for (int s = sim->h_ubody[u]; s < sim->h_ubody[u + 1]; s += 64) warps.push_back(make_int2(s, u));
     int e;
     if ((e = alloc_for(sim, n, nuniv, nnodes, (int)chunks.size(), (int)warps.size()))) return e;
     sim->nbody = n;
@@ -529,7 +545,8 @@ int nbh_load_batch(nbh_sim* sim, int32_t nuniv, const int32_t* counts, const flo
     sim->nnodes = nnodes;
     sim->ncells = nnodes + 1 - n;
     sim->nchunks = (int)chunks.size();
-    sim->nwarps = (int)warps.size();
+    sim->nwarps = nw32;
+    sim->nitems64 = (int)warps.size() - nw32;
     cudaStream_t s = sim->stream;
     CK(cudaMemcpyAsync(sim->ubody, sim->h_ubody.data(), sizeof(int) * (nuniv + 1), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(sim->chunks, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice, s));
@@ -893,7 +910,7 @@ int nbh_set_theta_model(nbh_sim* sim, const float* params, int32_t nparams, cons
     }
     if (!params || nparams != kMlpParams || !feat_mean || !feat_inv_std || !(theta_min > 0.0f) ||
         !(theta_max >= theta_min))
-        return fail(sim, NBH_ERR_MODEL, "model needs 4993 parameters, 12 means and inverse deviations, "
+        return fail(sim, NBH_ERR_MODEL, "model needs 5057 parameters, 12 means and inverse deviations, "
                                         "0 < theta_min <= theta_max");
     for (int i = 0; i < kMlpParams; ++i)
         if (!std::isfinite(params[i])) return fail(sim, NBH_ERR_MODEL, "non-finite model parameter");
@@ -912,6 +929,7 @@ int nbh_set_theta_model(nbh_sim* sim, const float* params, int32_t nparams, cons
     CK(cudaStreamSynchronize(s));
     const int since = sim->h_state->step + 1;
     CK(cudaMemcpyAsync(&sim->st->theta_since, &since, sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(&sim->st->theta_every, &sim->theta_every, sizeof(int), cudaMemcpyHostToDevice, s));
     const StepParams p = step_params(sim);
     std::vector<float> th((size_t)sim->nbody, std::sqrt(p.theta2));
     CK(cudaMemcpyAsync(sim->theta_body, th.data(), sizeof(float) * sim->nbody, cudaMemcpyHostToDevice, s));
@@ -919,6 +937,27 @@ int nbh_set_theta_model(nbh_sim* sim, const float* params, int32_t nparams, cons
     CK(cudaGetLastError());
     sim->theta_active = true;
     drop_graph(sim);
+    return NBH_OK;
+}
+
+int nbh_set_theta_interval(nbh_sim* sim, int32_t every) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (every < 1 || every > (1 << 20)) return fail(sim, NBH_ERR_INVALID, "theta interval must be in [1, 2^20]");
+    if (sim->loaded) {
+        CK(cudaSetDevice(sim->device));
+        CK(cudaMemcpyAsync(&sim->st->theta_every, &every, sizeof(int), cudaMemcpyHostToDevice, sim->stream));
+        CK(cudaStreamSynchronize(sim->stream));
+    }
+    if (every != sim->theta_every) drop_graph(sim);
+    sim->theta_every = every;
+    return NBH_OK;
+}
+
+int nbh_set_theta_grouping(nbh_sim* sim, int32_t group_min) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (group_min != 0 && group_min != 1) return fail(sim, NBH_ERR_INVALID, "grouping is 0 or 1");
+    if (group_min != sim->theta_group) drop_graph(sim);
+    sim->theta_group = group_min;
     return NBH_OK;
 }
 

@@ -53,7 +53,7 @@ struct DevState {
     int bbox_ticket;     // last-block ticket of the bbox stage (reference _blockCount)
     int force_next;      // work counter of the force stage
     int theta_since;     // learned theta: steps up to this index use the fixed theta
-    int pad1;
+    int theta_every;     // learned theta: steps between evaluations of the model (>= 1)
     unsigned long long interactions;   // accepted force evaluations of the last step
     unsigned long long pad2[3];
     // Build contention meters, spread over kDiagSlots addresses so that counting does not
@@ -86,9 +86,11 @@ struct StepParams {
     unsigned* ubox;      // nuniv * 6 ordered-int extents (min x,y,z, max x,y,z)
     float* uradius;      // nuniv root half-widths
     const int4* chunks;  // (universe, begin, end, 0) body chunks that never span universes
-    const int2* warps;   // (first sorted position, universe) of each force work item
+    const int2* warps;   // (first sorted position, universe) of each 32-body work item
+    const int2* items64; // the same for 64-body items (vote width 64)
     int nchunks;
     int nwarps;
+    int nitems64;
     int nbody;
     int nnodes;          // NUMBER_OF_NODES (top of the pool)
     int nuniv;
@@ -97,6 +99,9 @@ struct StepParams {
     float dt;
     float G;
     int precise;
+    int theta_group;     // per-body theta: 1 = each vote group walks with its smallest angle
+    int feat_gate;       // force launch gated on the learned-theta schedule: 0 none,
+                         // 1 run only on bound-recording steps, 2 only on the others
 };
 
 __device__ __forceinline__ int* cell_child(const StepParams& p, int c) {
@@ -106,6 +111,20 @@ __device__ __forceinline__ int* cell_child(const StepParams& p, int c) {
 // Raise an error once; later stages see status != 0 and return at entry.
 __device__ __forceinline__ void raise_error(DevState* st, int code) {
     atomicCAS(&st->status, 0, code);
+}
+
+// Learned opening angle schedule (steps >= theta_since, where theta_since is the first
+// step after the model was switched on): the walks of steps since, since + k, since + 2k,
+// ... record each body's error bound, and the model sets new angles on the step after
+// each of them (k = theta_every; with k = 1 every walk records and every later step
+// evaluates).  In between, bodies keep their angles and the walk records nothing.
+__device__ __forceinline__ bool theta_bound_step(const DevState* st, int step) {
+    const int k = st->theta_every > 0 ? st->theta_every : 1;
+    return (step - st->theta_since) % k == 0;
+}
+__device__ __forceinline__ bool theta_model_step(const DevState* st, int step) {
+    const int k = st->theta_every > 0 ? st->theta_every : 1;
+    return step > st->theta_since && (step - st->theta_since) % k == 1 % k;
 }
 
 __device__ __forceinline__ int load_status(const DevState* st) {

@@ -12,9 +12,16 @@ constexpr int kForceThreads = 128;
 constexpr int kStackCap = 256;
 constexpr int kFastMaxDepth = (kStackCap - 8) / 7 + 1;
 
+// Lanes of one vote group: W bodies on W lanes for W <= 32; W = 64 puts two bodies on
+// each lane of one warp.
+template <int W>
+__host__ __device__ constexpr int group_lanes() {
+    return W < 32 ? W : 32;
+}
+
 template <int W>
 constexpr size_t force_smem_bytes() {
-    return (size_t)(kForceThreads / W) * kStackCap * (sizeof(float4) + sizeof(int2));
+    return (size_t)(kForceThreads / group_lanes<W>()) * kStackCap * (sizeof(float4) + sizeof(int2));
 }
 
 // Opening threshold of tree level L (root = 0): r^2/theta^2 * 4^-L + eps^2
@@ -59,42 +66,54 @@ __device__ __forceinline__ float dist2(const float dx, const float dy, const flo
 }
 
 // -------------------------------------------------------------------------------------
-// Force (calculateforce.cl:52-185).  A group of W lanes (W = 32: one warp; W = 16: the
-// reference's work-group, :99,145) takes W consecutive bodies of the depth-first order and
-// walks its universe's tree.  A body child is always accepted; a cell child only if every
-// body of the group sees d^2 + eps^2 >= dq[level] (work_group_all, :145), else it is
-// opened.  The walk is depth-first in child order (children are compacted, so the first
-// empty slot ends a cell), so every body accumulates its interactions in the reference's
-// order.  Every lane of a group accepts the same children, so the group's interaction
-// count is counted once per opened cell, not per visit.
+// Force (calculateforce.cl:52-185).  A group of W bodies (W = 32: one warp; W = 16: the
+// reference's work-group, :99,145; W = 64: one warp with two bodies per lane) takes W
+// consecutive bodies of the depth-first order and walks its universe's tree.  A body
+// child is always accepted; a cell child only if every body of the group sees
+// d^2 + eps^2 >= dq[level] (work_group_all, :145), else it is opened.  The walk is
+// depth-first in child order (children are compacted, so the first empty slot ends a
+// cell), so every body accumulates its interactions in the reference's order.  Every lane
+// of a group accepts the same children, so the group's interaction count is counted once
+// per opened cell, not per visit.
 //
 // GB300 schedule: opening a cell loads its 8 child slots and the 8 node records that
 // summarize stored next to them (kids4) with one load per lane -- one round trip per
 // opened cell -- and pushes them, first child on top, onto the group's shared-memory
-// stack with their level factor 4^-level (-1 for bodies, which makes the test pass);
-// each visit reads one record from shared memory and needs no branch on its kind.  Lanes
-// past the end of a universe walk with their group's first body, so they never change a
-// vote and need no predicate.  Work items (32 bodies) are handed out dynamically.
-// After the walk: the leapfrog velocity correction for step > 0 (:174-181) and the
-// acceleration store (:183-185).
+// stack with their opening threshold (fixed angle: t0 * 4^-level + eps^2, formed once at
+// the push; per-body angle: the level factor 4^-level) or -1 for bodies, which makes the
+// test pass; each visit reads one record from shared memory and needs no branch on its
+// kind.  With W = 64 every stack pop, vote and cell opening serves two bodies per lane.
+// Lanes past the end of a universe walk with their group's first body, so they never
+// change a vote and need no predicate.  Work items (32 bodies; 64 for W = 64) are handed
+// out dynamically.  After the walk: the leapfrog velocity correction for step > 0
+// (:174-181) and the acceleration store (:183-185).
 //
 // REF: reference arithmetic (rounded products, 1/sqrt correctly rounded); otherwise FMA and
-// the hardware inverse square root.  PB: per-body opening angle from theta_body.  FEAT:
+// the hardware inverse square root.  PB: per-body opening angle from theta_body (with
+// p.theta_group, the smallest angle of the group for all its bodies).  FEAT:
 // also accumulate each body's quadrupole error bound into acc.w.  With p.probe set the
-// results go to p.probe (x, y, z, bound) and no body state changes (force probe).
+// results go to p.probe (x, y, z, bound) and no body state changes (force probe).  With
+// p.feat_gate set, a launch that does not match the step's place in the learned-theta
+// schedule returns at once (the step graph holds a recording and a plain launch).
 template <int W, bool REF, bool PB, bool FEAT>
 __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
     if (load_status(p.st)) return;
-    constexpr int kGroups = kForceThreads / W;
+    if (p.feat_gate && theta_bound_step(p.st, p.st->step) != (p.feat_gate == 1)) return;
+    constexpr int GL = group_lanes<W>();            // lanes per group
+    constexpr int BPL = W / GL;                     // bodies per lane
+    constexpr int kGroups = kForceThreads / GL;
+    // The stack entry carries the finished threshold when it is the same for every body
+    // of the group (fixed angle) and nothing else needs the level factor.
+    constexpr bool kStoreDq = !PB && !FEAT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float4* const sq_all = reinterpret_cast<float4*>(smem_raw);
     int2* const se_all = reinterpret_cast<int2*>(sq_all + kGroups * kStackCap);
     const int lane = threadIdx.x & 31;
-    const int grp = threadIdx.x / W;
-    const int glane = threadIdx.x % W;
-    const unsigned gmask = (W == 32) ? 0xffffffffu : (0xffffu << (16 * (lane >> 4)));
+    const int grp = threadIdx.x / GL;
+    const int glane = threadIdx.x % GL;
+    const unsigned gmask = (GL == 32) ? 0xffffffffu : (0xffffu << (16 * (lane >> 4)));
     float4* const sq = sq_all + grp * kStackCap;     // node record of each pending child
-    int2* const se = se_all + grp * kStackCap;       // (node index, bits of 4^-level or -1)
+    int2* const se = se_all + grp * kStackCap;       // (node index, bits of threshold or level factor)
     int* const snode = reinterpret_cast<int*>(se);   // deep-tree walk: (cell, next) per level
     int* const snext = snode + kMaxDepth;
     const int nbody = p.nbody;
@@ -104,31 +123,55 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
     const float4* __restrict__ node4 = p.node4;
     const int* __restrict__ child = p.child;
     const float4* __restrict__ kids4 = p.kids4;
+    const int2* __restrict__ items = BPL == 2 ? p.items64 : p.warps;
+    const int nitems = BPL == 2 ? p.nitems64 : p.nwarps;
     unsigned long long my_inter = 0;
 
     for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(&p.st->force_next, 1);
         item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= p.nwarps) break;
-        const int2 wi = p.warps[item];
+        if (item >= nitems) break;
+        const int2 wi = items[item];
         const int u = wi.y;
-        const int s = wi.x + lane;
-        const bool valid = s < p.ubody[u + 1];
+        const int uend = p.ubody[u + 1];
         // Lanes past the universe's end take their group's first body.
-        const int sg = valid ? s : wi.x + (lane / W) * W;
-        const bool gvalid = sg < p.ubody[u + 1];       // the group has any body at all
-        const int b = gvalid ? p.sorted[sg] : 0;
-        const float4 pb = node4[b];
+        const int gfirst = wi.x + (GL < 32 ? (lane / GL) * GL : 0);
+        const bool gvalid = gfirst < uend;       // the group has any body at all
         const float r = p.uradius[u];
         const float rr = __fmul_rn(r, r);
-        float th2 = p.theta2;
-        if constexpr (PB) {
-            const float th = p.theta_body[b];
-            th2 = __fmul_rn(th, th);
+        bool valid[BPL];
+        int b[BPL];
+        float4 pb[BPL];
+        float t0[BPL];
+        float ax[BPL], ay[BPL], az[BPL], eb[BPL];
+#pragma unroll
+        for (int k = 0; k < BPL; ++k) {
+            const int sk = wi.x + 32 * k + lane;
+            valid[k] = sk < uend;
+            b[k] = gvalid ? p.sorted[valid[k] ? sk : gfirst] : 0;
+            pb[k] = node4[b[k]];
+            float th2 = p.theta2;
+            if constexpr (PB) {
+                const float th = p.theta_body[b[k]];
+                th2 = __fmul_rn(th, th);
+            }
+            t0[k] = th2 > 0.0f ? __fdiv_rn(rr, th2) : rr;
+            ax[k] = ay[k] = az[k] = eb[k] = 0.f;
         }
-        const float t0 = th2 > 0.0f ? __fdiv_rn(rr, th2) : rr;
-        float ax = 0.f, ay = 0.f, az = 0.f, eb = 0.f;
+        if constexpr (PB) {
+            if (p.theta_group) {
+                // the group walks with its smallest angle (largest r^2 / theta^2), the walk
+                // of a fixed angle; lanes past the end hold the first body's angle
+                float tm = t0[0];
+#pragma unroll
+                for (int k = 1; k < BPL; ++k) tm = fmaxf(tm, t0[k]);
+#pragma unroll
+                for (int o = GL / 2; o > 0; o >>= 1) tm = fmaxf(tm, __shfl_xor_sync(gmask, tm, o));
+#pragma unroll
+                for (int k = 0; k < BPL; ++k) t0[k] = tm;
+            }
+        }
         long long ninter = 0;
         const int root = p.nnodes - u;
 
@@ -140,78 +183,107 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
                 float open_s = 1.0f;                      // 4^-level of open's children
                 bool ok = true;
                 for (;;) {
-                    if (open >= 0) {
-                        // push the children of `open`, first child on top
-                        int chk = kNull;
-                        float4 qk = make_float4(0.f, 0.f, 0.f, 0.f);
-                        if (glane < 8) {
-                            const size_t o8 = ((size_t)(open - nbody) << 3) + glane;
-                            chk = __ldg(child + o8);
-                            qk = __ldg(kids4 + o8);
+                    // push the children of `open`, first child on top
+                    int chk = kNull;
+                    float4 qk = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (glane < 8) {
+                        const size_t o8 = ((size_t)(open - nbody) << 3) + glane;
+                        chk = __ldg(child + o8);
+                        qk = __ldg(kids4 + o8);
+                    }
+                    float tag = open_s;
+                    if constexpr (kStoreDq) {
+                        // level factor of open's children, 4^-level(open), exact; the same
+                        // threshold the visit would form from it
+                        const int lv = __ldg(p.clevel + (open - nbody));
+                        tag = __fadd_rn(__fmul_rn(t0[0], __int_as_float((127 - 2 * lv) << 23)), eps2);
+                    }
+                    const unsigned bal = __ballot_sync(gmask, glane < 8 && chk >= 0) & gmask;
+                    const int cnt = __popc(bal);
+                    if (top + cnt > kStackCap) {           // unreachable below kFastMaxDepth
+                        raise_error(p.st, NBH_ERR_DEPTH);
+                        ok = false;
+                        break;
+                    }
+                    if (glane < cnt) {
+                        const int slot = top + cnt - 1 - glane;
+                        sq[slot] = qk;
+                        se[slot] = make_int2(chk, __float_as_int(chk >= nbody ? tag : -1.0f));
+                    }
+                    top += cnt;
+                    pushed += cnt;
+                    ++opened;
+                    __syncwarp(gmask);
+                    // visit until a cell has to be opened or the stack is empty
+                    open = -1;
+                    while (top > 0) {
+                        --top;
+                        const int2 e = se[top];
+                        const float4 q = sq[top];
+                        const float sl = __int_as_float(e.y);
+                        float dx[BPL], dy[BPL], dz[BPL], d2[BPL];
+                        bool pass = true;
+#pragma unroll
+                        for (int k = 0; k < BPL; ++k) {
+                            dx[k] = __fsub_rn(q.x, pb[k].x);
+                            dy[k] = __fsub_rn(q.y, pb[k].y);
+                            dz[k] = __fsub_rn(q.z, pb[k].z);
+                            d2[k] = dist2<REF>(dx[k], dy[k], dz[k], eps2);
+                            const float dq = kStoreDq ? sl : __fadd_rn(__fmul_rn(t0[k], sl), eps2);
+                            pass = pass && d2[k] >= dq;
                         }
-                        const unsigned bal = __ballot_sync(gmask, glane < 8 && chk >= 0) & gmask;
-                        const int cnt = __popc(bal);
-                        if (top + cnt > kStackCap) {           // unreachable below kFastMaxDepth
-                            raise_error(p.st, NBH_ERR_DEPTH);
-                            ok = false;
+                        if (__all_sync(gmask, pass)) {
+                            const float s2 = FEAT ? __fmul_rn(rr, fmaxf(sl, 0.0f)) : 0.0f;
+#pragma unroll
+                            for (int k = 0; k < BPL; ++k)
+                                interact<REF, FEAT>(q, dx[k], dy[k], dz[k], d2[k], ax[k], ay[k], az[k], eb[k], s2);
+                        } else {
+                            open = e.x;
+                            if constexpr (!kStoreDq) open_s = __fmul_rn(sl, 0.25f);
                             break;
                         }
-                        if (glane < cnt) {
-                            const int slot = top + cnt - 1 - glane;
-                            sq[slot] = qk;
-                            se[slot] = make_int2(chk, __float_as_int(chk >= nbody ? open_s : -1.0f));
-                        }
-                        top += cnt;
-                        pushed += cnt;
-                        ++opened;
-                        open = -1;
-                        __syncwarp(gmask);
                     }
-                    if (top == 0) break;
-                    --top;
-                    const int2 e = se[top];
-                    const float4 q = sq[top];
-                    const float dx = __fsub_rn(q.x, pb.x);
-                    const float dy = __fsub_rn(q.y, pb.y);
-                    const float dz = __fsub_rn(q.z, pb.z);
-                    const float d2 = dist2<REF>(dx, dy, dz, eps2);
-                    const float sl = __int_as_float(e.y);
-                    const float dq = __fadd_rn(__fmul_rn(t0, sl), eps2);
-                    if (__all_sync(gmask, d2 >= dq)) {
-                        interact<REF, FEAT>(q, dx, dy, dz, d2, ax, ay, az, eb, __fmul_rn(rr, fmaxf(sl, 0.0f)));
-                    } else {
-                        open = e.x;
-                        open_s = __fmul_rn(sl, 0.25f);
-                        __syncwarp(gmask);     // every lane has read the stack before it is refilled
-                    }
+                    if (open < 0) break;
+                    __syncwarp(gmask);     // every lane has read the stack before it is refilled
                 }
                 if (ok) ninter = pushed - opened;
             } else {
                 // Deep trees: per-level (cell, next child) walk (calculateforce.cl:112-172).
                 int depth = 0;
                 int node = root;
-                int k = 0;
-                float dq = level_dq(t0, 0, eps2);
+                int k8 = 0;
+                float dq[BPL];
+#pragma unroll
+                for (int k = 0; k < BPL; ++k) dq[k] = level_dq(t0[k], 0, eps2);
                 for (;;) {
                     int ch = kNull;
-                    if (k < 8) ch = __ldg(child + ((size_t)(node - nbody) << 3) + k);
+                    if (k8 < 8) ch = __ldg(child + ((size_t)(node - nbody) << 3) + k8);
                     if (ch < 0) {
                         if (depth == 0) break;
                         --depth;
                         node = snode[depth];
-                        k = snext[depth];
-                        dq = level_dq(t0, depth, eps2);
+                        k8 = snext[depth];
+#pragma unroll
+                        for (int k = 0; k < BPL; ++k) dq[k] = level_dq(t0[k], depth, eps2);
                         continue;
                     }
-                    ++k;
+                    ++k8;
                     const float4 q = __ldg(node4 + ch);
-                    const float dx = __fsub_rn(q.x, pb.x);
-                    const float dy = __fsub_rn(q.y, pb.y);
-                    const float dz = __fsub_rn(q.z, pb.z);
-                    const float d2 = dist2<REF>(dx, dy, dz, eps2);
-                    if (ch < nbody || __all_sync(gmask, d2 >= dq)) {
-                        interact<REF, FEAT>(q, dx, dy, dz, d2, ax, ay, az, eb,
-                                            ch >= nbody ? ldexpf(rr, -2 * depth) : 0.0f);
+                    float dx[BPL], dy[BPL], dz[BPL], d2[BPL];
+                    bool pass = true;
+#pragma unroll
+                    for (int k = 0; k < BPL; ++k) {
+                        dx[k] = __fsub_rn(q.x, pb[k].x);
+                        dy[k] = __fsub_rn(q.y, pb[k].y);
+                        dz[k] = __fsub_rn(q.z, pb[k].z);
+                        d2[k] = dist2<REF>(dx[k], dy[k], dz[k], eps2);
+                        pass = pass && d2[k] >= dq[k];
+                    }
+                    if (ch < nbody || __all_sync(gmask, pass)) {
+                        const float s2 = ch >= nbody ? ldexpf(rr, -2 * depth) : 0.0f;
+#pragma unroll
+                        for (int k = 0; k < BPL; ++k)
+                            interact<REF, FEAT>(q, dx[k], dy[k], dz[k], d2[k], ax[k], ay[k], az[k], eb[k], s2);
                         ++ninter;
                     } else {
                         if (depth + 1 >= kMaxDepth) {   // unreachable for a tree the build accepted
@@ -220,54 +292,52 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
                         }
                         // every lane writes the same entry, so no lane reads a stale one
                         snode[depth] = node;
-                        snext[depth] = k;
+                        snext[depth] = k8;
                         ++depth;
                         node = ch;
-                        k = 0;
-                        dq = level_dq(t0, depth, eps2);
+                        k8 = 0;
+#pragma unroll
+                        for (int k = 0; k < BPL; ++k) dq[k] = level_dq(t0[k], depth, eps2);
                     }
                 }
             }
         }
 
-        if (valid && p.probe) {
+#pragma unroll
+        for (int k = 0; k < BPL; ++k) {
+            if (!valid[k]) continue;
             if (p.G != 1.0f) {
-                ax = __fmul_rn(ax, p.G);
-                ay = __fmul_rn(ay, p.G);
-                az = __fmul_rn(az, p.G);
-                eb = __fmul_rn(eb, p.G);
+                ax[k] = __fmul_rn(ax[k], p.G);
+                ay[k] = __fmul_rn(ay[k], p.G);
+                az[k] = __fmul_rn(az[k], p.G);
+                eb[k] = __fmul_rn(eb[k], p.G);
             }
-            p.probe[b] = make_float4(ax, ay, az, eb);
             my_inter += (unsigned long long)ninter;
-        } else if (valid) {
-            if (p.G != 1.0f) {
-                ax = __fmul_rn(ax, p.G);
-                ay = __fmul_rn(ay, p.G);
-                az = __fmul_rn(az, p.G);
-                eb = __fmul_rn(eb, p.G);
+            if (p.probe) {
+                p.probe[b[k]] = make_float4(ax[k], ay[k], az[k], eb[k]);
+                continue;
             }
-            float4 v = p.vel[b];
-            const float4 ao = p.acc[b];
+            float4 v = p.vel[b[k]];
+            const float4 ao = p.acc[b[k]];
             if (step > 0) {
-                const float tx = __fmul_rn(__fsub_rn(ax, ao.x), p.dt);
-                const float ty = __fmul_rn(__fsub_rn(ay, ao.y), p.dt);
-                const float tz = __fmul_rn(__fsub_rn(az, ao.z), p.dt);
+                const float tx = __fmul_rn(__fsub_rn(ax[k], ao.x), p.dt);
+                const float ty = __fmul_rn(__fsub_rn(ay[k], ao.y), p.dt);
+                const float tz = __fmul_rn(__fsub_rn(az[k], ao.z), p.dt);
                 if (p.precise) {
-                    float4 kv = p.kvel[b];
+                    float4 kv = p.kvel[b[k]];
                     float y1, t1;
                     y1 = __fsub_rn(__fmul_rn(tx, 0.5f), kv.x); t1 = __fadd_rn(v.x, y1); kv.x = __fsub_rn(__fsub_rn(t1, v.x), y1); v.x = t1;
                     y1 = __fsub_rn(__fmul_rn(ty, 0.5f), kv.y); t1 = __fadd_rn(v.y, y1); kv.y = __fsub_rn(__fsub_rn(t1, v.y), y1); v.y = t1;
                     y1 = __fsub_rn(__fmul_rn(tz, 0.5f), kv.z); t1 = __fadd_rn(v.z, y1); kv.z = __fsub_rn(__fsub_rn(t1, v.z), y1); v.z = t1;
-                    p.kvel[b] = kv;
+                    p.kvel[b[k]] = kv;
                 } else {
                     v.x = madd<REF>(tx, 0.5f, v.x);
                     v.y = madd<REF>(ty, 0.5f, v.y);
                     v.z = madd<REF>(tz, 0.5f, v.z);
                 }
-                p.vel[b] = v;
+                p.vel[b[k]] = v;
             }
-            p.acc[b] = make_float4(ax, ay, az, eb);
-            my_inter += (unsigned long long)ninter;
+            p.acc[b[k]] = make_float4(ax[k], ay[k], az[k], eb[k]);
         }
         __syncwarp();
     }
@@ -308,6 +378,7 @@ static cudaError_t prep_force_w() {
 
 int prepare_force_kernels() {
     cudaError_t e = cudaSuccess, t;
+    if ((t = prep_force_w<64, false>()) != cudaSuccess) e = t;
     if ((t = prep_force_w<32, false>()) != cudaSuccess) e = t;
     if ((t = prep_force_w<32, true>()) != cudaSuccess) e = t;
     if ((t = prep_force_w<16, false>()) != cudaSuccess) e = t;
@@ -317,7 +388,9 @@ int prepare_force_kernels() {
 
 void launch_force(const StepParams& p, int vote, bool ref, bool feat, int grid, cudaStream_t s) {
     const bool pb = p.theta_body != nullptr;
-    if (vote == 16) {
+    if (vote == 64) {
+        launch_force_t<64, false>(p, pb, feat, grid, s);   // FMA arithmetic only
+    } else if (vote == 16) {
         if (ref) launch_force_t<16, true>(p, pb, feat, grid, s);
         else launch_force_t<16, false>(p, pb, feat, grid, s);
     } else {
@@ -327,7 +400,10 @@ void launch_force(const StepParams& p, int vote, bool ref, bool feat, int grid, 
 }
 
 int occupancy_force(int vote, bool ref, int* blocks_per_sm) {
-    const size_t s16 = force_smem_bytes<16>(), s32 = force_smem_bytes<32>();
+    const size_t s16 = force_smem_bytes<16>(), s32 = force_smem_bytes<32>(), s64 = force_smem_bytes<64>();
+    if (vote == 64)
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<64, false, false, false>,
+                                                             kForceThreads, s64);
     if (vote == 16)
         return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, true, false, false>, kForceThreads, s16)
                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, false, false, false>, kForceThreads, s16);

@@ -7,7 +7,7 @@ namespace nbh {
 struct StepParams;
 
 void launch_bbox(const StepParams& p, int grid, cudaStream_t s);
-void launch_build(const StepParams& p, int grid, cudaStream_t s);
+void launch_build(const StepParams& p, cudaStream_t s);
 void launch_link(const StepParams& p, int grid, cudaStream_t s);
 void launch_summarize(const StepParams& p, bool ref, int grid, cudaStream_t s);
 void launch_sort(const StepParams& p, int grid, cudaStream_t s);

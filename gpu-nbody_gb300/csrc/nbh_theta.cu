@@ -189,6 +189,7 @@ __global__ void __launch_bounds__(kThetaThreads) theta_kernel(StepParams p, cons
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int step = p.st->step;
     const bool use_fixed = step <= p.st->theta_since;   // no previous walk with bounds yet
+    if (!use_fixed && !theta_model_step(p.st, step)) return;   // angles kept from the last evaluation
     const float fixed = sqrtf(p.theta2);
     if (!use_fixed) load_model(S, m);
     __syncthreads();

@@ -128,17 +128,38 @@ __global__ void __launch_bounds__(256) bbox_kernel(StepParams p) {
 // one release store into the locked slot (:173-180), which orders every write made under
 // the lock.  Failed locks retry from the same node (the tree only grows) with a bounded,
 // backed-off wait.
-__global__ void __launch_bounds__(256) build_kernel(StepParams p) {
+//
+// Insertion runs in three phases (three launches): first one body of every 256-body
+// chunk, then one in 16, then the rest.  The octree of a set of bodies does not depend
+// on the order the bodies arrive in, so the phases build exactly the tree a single pass
+// would; what they change is contention.  In one pass every body of a universe that is
+// resident at once descends into the same empty top levels and waits on each split there
+// in turn (in a batch of small universes that is every body).  After the first two
+// phases the top of each tree already holds about 1/16 of its bodies, so the last phase's
+// descents spread over many cells and rarely meet a locked slot.
+constexpr int kBuildPhases = 3;
+__host__ __device__ constexpr int phase_bodies(int phase) {   // per full 256-body chunk
+    return phase == 0 ? 1 : (phase == 1 ? 15 : 240);
+}
+// Offset inside its chunk of the phase's idx-th body: 0; 16, 32, ..., 240; the rest.
+__device__ __forceinline__ int phase_offset(int phase, int idx) {
+    return phase == 0 ? 0 : (phase == 1 ? 16 * (idx + 1) : idx + idx / 15 + 1);
+}
+
+__global__ void __launch_bounds__(256) build_kernel(StepParams p, int phase) {
     if (load_status(p.st)) return;
     int local_max = 1;
     int waits = 0, misses = 0;
     const int nbody = p.nbody;
-    for (int ci = blockIdx.x; ci < p.nchunks; ci += gridDim.x) {
-        const int4 ck = p.chunks[ci];
-        const int root = p.nnodes - ck.x;
-        const float4 rc = p.node4[root];
-        const float radius = p.uradius[ck.x];
-        for (int b = ck.y + threadIdx.x; b < ck.z; b += blockDim.x) {
+    const int per = phase_bodies(phase);
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;   // one body per thread
+    if (g < (long long)p.nchunks * per) {
+        const int4 ck = p.chunks[g / per];
+        const int b = ck.y + phase_offset(phase, (int)(g % per));
+        if (b < ck.z) {
+            const int root = p.nnodes - ck.x;
+            const float4 rc = p.node4[root];
+            const float radius = p.uradius[ck.x];
             const float4 bp = p.node4[b];
             int node = root, depth = 1;
             float r = radius;
@@ -149,7 +170,7 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
             // rest of the build, and each cell's slots are one 32-byte sector first read
             // after the cell was published, so a cell index read from L1 is always right;
             // any other value is only acted on through the CAS below, which fails if it is
-            // stale and returns the current value.  This keeps the 1M descents off the L2
+            // stale and returns the current value.  This keeps the descents off the L2
             // lines of the top cells.
             int ch = __ldca(slot);
             for (;;) {
@@ -231,9 +252,8 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p) {
                     ch = seen;
                     continue;
                 }
-                // the slot is locked by a split in progress: wait (bounded, backed off:
-                // thousands of descents may wait on the same few slots near the root early
-                // in the build) until it holds the new subtree
+                // the slot is locked by a split in progress: wait (bounded, backed off)
+                // until it holds the new subtree
                 ch = bounded_wait_ne(slot, kLock, kWaitNs, p.st, kBackoffMinNs, &waits);
                 if (ch == kLock) goto finish;
             }
@@ -421,8 +441,11 @@ void launch_bbox(const StepParams& p, int grid, cudaStream_t s) {
     if (p.precise) bbox_kernel<true><<<grid, 256, 0, s>>>(p);
     else bbox_kernel<false><<<grid, 256, 0, s>>>(p);
 }
-void launch_build(const StepParams& p, int grid, cudaStream_t s) {
-    build_kernel<<<grid, 256, 0, s>>>(p);
+void launch_build(const StepParams& p, cudaStream_t s) {
+    for (int phase = 0; phase < kBuildPhases; ++phase) {
+        const long long bodies = (long long)p.nchunks * phase_bodies(phase);
+        build_kernel<<<(unsigned)((bodies + 255) / 256), 256, 0, s>>>(p, phase);
+    }
 }
 void launch_link(const StepParams& p, int grid, cudaStream_t s) {
     link_kernel<<<grid, 256, 0, s>>>(p);

@@ -25,7 +25,7 @@ NBH_ERR_MODEL = -9
 NBH_MAXDEPTH = 64
 NBH_ARITH_FMA = 0
 NBH_ARITH_REFERENCE = 1
-NBH_MLP_PARAMS = 4993
+NBH_MLP_PARAMS = 5057
 NBH_MLP_FEATURES = 12
 NBH_DIRECT_STATIC_MAX = 65536
 
@@ -99,6 +99,8 @@ SIGNATURES = {
     "nbh_generate_rotating_disk": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_float, C.c_float,
                                              C.c_float] + [_P] * 7),
     "nbh_set_theta_model": (C.c_int, [_P, _P, C.c_int32, _P, _P, C.c_float, C.c_float, C.c_int32]),
+    "nbh_set_theta_interval": (C.c_int, [_P, C.c_int32]),
+    "nbh_set_theta_grouping": (C.c_int, [_P, C.c_int32]),
     "nbh_read_theta": (C.c_int, [_P, _P]),
     "nbh_force_probe": (C.c_int, [_P, _P, _P, _P, _P, _P, C.POINTER(C.c_int64)]),
     "nbh_theta_features": (C.c_int, [_P, _P, C.c_int32]),

@@ -47,18 +47,28 @@ def features(sim, use_probe=True):
     return f
 
 
-def theta_target(E, tau, grid=GRID, floor=0.3):
+def theta_target(E, tau, grid=GRID, floor=0.3, monotone=True):
     """Largest angle with error <= tau per sample (columns of E, rows = grid angles), log-
-    linearly interpolated between grid points; `floor` when even the smallest fails."""
+    linearly interpolated between grid points; `floor` when even the smallest fails.
+    monotone: the largest angle below which every grid angle meets tau (a body's error is
+    not monotone in the angle -- cancellations make single angles pass by luck, and such
+    a pass does not carry over to a walk with another angle); otherwise the largest
+    passing grid angle."""
     lE = np.log(np.maximum(E, 1e-300))
     lt = np.log(np.asarray(grid))
     lt_tau = np.log(tau)
     out = np.full(E.shape[1], np.log(floor))
     for j in range(E.shape[1]):
-        ok = np.where(lE[:, j] <= lt_tau)[0]
-        if ok.size == 0:
-            continue
-        k = ok.max()
+        passing = lE[:, j] <= lt_tau
+        if monotone:
+            k = int(np.argmin(passing)) - 1 if not passing.all() else len(grid) - 1
+            if k < 0:
+                continue
+        else:
+            ok = np.where(passing)[0]
+            if ok.size == 0:
+                continue
+            k = ok.max()
         if k == len(grid) - 1:
             out[j] = lt[-1]
             continue
@@ -107,7 +117,21 @@ def train(X, Y, quantile=0.2, iters=1500, lr=3e-3, seed=0, device=0, std_floor=0
             "quantile": float(quantile)}
 
 
-def install(sim, model, theta_min=0.3, theta_max=1.0, enable=True):
+def set_grouping(sim, group_min):
+    """1: each vote group walks with the smallest angle of its bodies; 0: per body."""
+    sim._check(sim._L.nbh_set_theta_grouping(sim._h, int(bool(group_min))))
+
+
+def install(sim, model, theta_min=0.3, theta_max=1.0, enable=True, every=None, group=None):
+    """Switch the model on in `sim`; `every` = steps between evaluations, `group` = the
+    grouping of nbh_set_theta_grouping (defaults: the model's own "every" and "group"
+    entries, else 1 and 0)."""
+    if every is None:
+        every = int(model.get("every", 1))
+    if group is None:
+        group = int(model.get("group", 0))
+    sim._check(sim._L.nbh_set_theta_interval(sim._h, int(every)))
+    set_grouping(sim, group)
     p = np.ascontiguousarray(model["params"], dtype=np.float32)
     mu = np.ascontiguousarray(model["mean"], dtype=np.float32)
     inv = np.ascontiguousarray(model["inv_std"], dtype=np.float32)

@@ -32,7 +32,7 @@ def _f32(a):
     return None if a is None else np.ascontiguousarray(a, dtype=np.float32)
 
 
-def make_config(theta=0.5, eps=0.05, dt=0.025, G=1.0, pool_factor=2.0, vote_width=32,
+def make_config(theta=0.5, eps=0.05, dt=0.025, G=1.0, pool_factor=2.0, vote_width=None,
                 arith=L.NBH_ARITH_FMA, precise=False, stage_timing=False, use_graph=True,
                 device=0, theta2=0.0, eps2=0.0) -> L.NbhConfig:
     cfg = L.NbhConfig()
@@ -41,7 +41,8 @@ def make_config(theta=0.5, eps=0.05, dt=0.025, G=1.0, pool_factor=2.0, vote_widt
     cfg.theta, cfg.eps, cfg.dt, cfg.G = theta, eps, dt, G
     cfg.theta2, cfg.eps2 = theta2, eps2
     cfg.pool_factor = pool_factor
-    cfg.vote_width = vote_width
+    if vote_width is not None:          # None: the library default (64)
+        cfg.vote_width = vote_width
     cfg.arith = arith
     cfg.precise = int(bool(precise))
     cfg.stage_timing = int(bool(stage_timing))

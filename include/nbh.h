@@ -75,8 +75,9 @@ typedef struct nbh_config {
     float   G;             /* gravitational constant, multiplies every mass (reference: 1) */
     float   pool_factor;   /* node pool = max(pool_factor*N, 16384) rounded up to 16;
                               the reference uses 2.0 (calculateNumberOfNodes) */
-    int32_t vote_width;    /* bodies voting together on opening a cell: 32 (one warp,
-                              default) or 16 (the reference work-group, calculateforce.cl:145) */
+    int32_t vote_width;    /* bodies voting together on opening a cell: 64 (two bodies on
+                              each lane of one warp, default; FMA arithmetic), 32 (one warp)
+                              or 16 (the reference work-group, calculateforce.cl:145) */
     int32_t arith;         /* NBH_ARITH_FMA or NBH_ARITH_REFERENCE */
     int32_t precise;       /* 1: Kahan-compensated position/velocity updates and FP64
                               extent / root centre of mass; 0: reference arithmetic */
@@ -86,7 +87,7 @@ typedef struct nbh_config {
 } nbh_config;
 
 /* Fills *cfg with the defaults: theta 0.5, eps 0.05, dt 0.025, G 1, pool 2.0,
- * vote 32, FMA arithmetic, precise 0, stage timing 0, graph 1. */
+ * vote 64, FMA arithmetic, precise 0, stage timing 0, graph 1. */
 void nbh_config_default(nbh_config* cfg);
 
 typedef struct nbh_stats {
@@ -204,20 +205,34 @@ int nbh_direct_f64(nbh_sim* sim, int32_t nidx, const int32_t* idx,
 
 /* Installs an MLP 12->64->64->1 (ReLU; row-major FP32 parameters W1[64][12], b1[64],
  * W2[64][64], b2[64], W3[64], b3: NBH_MLP_PARAMS floats) and the normalisation of its 12
- * features (mean[12], inv_std[12]).  Every step then sets each body's opening angle to
- * clamp(exp(MLP((f - mean) * inv_std)), theta_min, theta_max), evaluated with BF16 weights
- * on the tensor cores, and the force walk records each body's quadrupole error bound for
- * the next step's features.  The first step after switching on walks with the fixed
+ * features (mean[12], inv_std[12]).  Every step (or every k-th, nbh_set_theta_interval)
+ * then sets each body's opening angle to clamp(exp(MLP((f - mean) * inv_std)), theta_min,
+ * theta_max), evaluated with BF16 weights on the tensor cores, and the force walk before
+ * it records each body's quadrupole error bound for the features.  The first step after switching on walks with the fixed
  * theta.  enable = 0 returns to the fixed theta.  Features (nbh_theta_features order):
  * log10|a|, log10(bound/|a|), log10(theta of the last walk), log10(d/R), log10(n_leaf+1),
  * level(leaf)/20, log10(n_leaf_parent+1), log10(n_leaf/h^3), log10(m_leaf/M),
  * log10(|a| d^2/M), log10(eps/h), log10(h/d); d = distance to the universe's centre of
  * mass, R, M = root half-width and mass, h = half-width of the cell holding the body. */
-#define NBH_MLP_PARAMS 4993
+#define NBH_MLP_PARAMS 5057
 #define NBH_MLP_FEATURES 12
 int nbh_set_theta_model(nbh_sim* sim, const float* params, int32_t nparams,
                         const float* feat_mean, const float* feat_inv_std,
                         float theta_min, float theta_max, int32_t enable);
+
+/* Evaluate the opening-angle model every `every` steps (1 <= every <= 2^20; default 1).
+ * The walk of the step before each evaluation records the error bounds the features
+ * need; the walks in between keep each body's angle and record nothing, so they run at
+ * the cost of a plain per-body-angle walk.  May be called before or after
+ * nbh_set_theta_model.  No counterpart in the reference (its opening angle is the
+ * compile-time THETA, calculateforce.cl:14). */
+int nbh_set_theta_interval(nbh_sim* sim, int32_t every);
+
+/* How a vote group uses its bodies' angles: 0 (default) every body tests a cell with its
+ * own angle and the group opens it unless all accept; 1 the group walks with the
+ * smallest angle among its bodies (a fixed-angle walk per group).  Applies to the
+ * learned angle and to nbh_force_probe.  No counterpart in the reference. */
+int nbh_set_theta_grouping(nbh_sim* sim, int32_t group_min);
 
 /* Writes the per-body opening angle of the last step into theta[N] (host). */
 int nbh_read_theta(nbh_sim* sim, float* theta);

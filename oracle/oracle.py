@@ -40,6 +40,7 @@ class _RbSim(C.Structure):
         ("radius", C.c_float),
         ("bottom", C.c_int), ("maxdepth", C.c_int), ("step", C.c_int), ("error", C.c_int),
         ("interactions", C.c_longlong),
+        ("theta_group", C.c_int),
     ]
 
 
@@ -61,6 +62,7 @@ def lib():
         L.rb_load.argtypes = [P] + [C.c_void_p] * 7
         L.rb_set_theta_body.argtypes = [P, C.c_void_p]
         L.rb_enable_ebound.argtypes = [P, C.c_int]
+        L.rb_set_theta_group.argtypes = [P, C.c_int]
         for fn in ("rb_bbox", "rb_build", "rb_summarize", "rb_sort", "rb_force",
                    "rb_integrate", "rb_step", "rb_tree"):
             getattr(L, fn).argtypes = [P]
@@ -124,6 +126,9 @@ class Oracle:
             t = np.ascontiguousarray(theta, dtype=np.float32)
             assert t.shape == (self.n,)
             lib().rb_set_theta_body(self._p, t.ctypes.data)
+
+    def set_theta_group(self, on=True):
+        lib().rb_set_theta_group(self._p, int(bool(on)))
 
     def enable_ebound(self, on=True):
         lib().rb_enable_ebound(self._p, int(bool(on)))

@@ -119,6 +119,8 @@ void rb_enable_ebound(rb_sim* s, int enable) {
     if (!enable) { free(s->ebound); s->ebound = NULL; }
 }
 
+void rb_set_theta_group(rb_sim* s, int on) { s->theta_group = on ? 1 : 0; }
+
 void rb_set_theta_body(rb_sim* s, const float* theta) {
     if (!theta) {
         free(s->theta_body);
@@ -353,6 +355,12 @@ int rb_force(rb_sim* s) {
             } else {
                 t0[k] = t0fixed;
             }
+        }
+        if (s->theta_body && s->theta_group) {
+            /* the group walks with its smallest angle (largest r^2/theta^2) */
+            float tm = t0[0];
+            for (int k = 1; k < cnt; ++k) tm = t0[k] > tm ? t0[k] : tm;
+            for (int k = 0; k < cnt; ++k) t0[k] = tm;
         }
         int snode[RB_MAXDEPTH + 2], snext[RB_MAXDEPTH + 2];
         int depth = 0;

@@ -40,6 +40,8 @@ typedef struct rb_sim {
     float radius;
     int bottom, maxdepth, step, error;
     long long interactions;
+    int theta_group;                /* per-body theta: 1 = each vote group walks with the
+                                       smallest angle of its bodies */
 } rb_sim;
 
 int rb_number_of_nodes(int n, float pool_factor);
@@ -51,6 +53,7 @@ void rb_load(rb_sim* s, const float* x, const float* y, const float* z,
              const float* vx, const float* vy, const float* vz, const float* m);
 void rb_set_theta_body(rb_sim* s, const float* theta);   /* NULL: fixed theta */
 void rb_enable_ebound(rb_sim* s, int enable);   /* accumulate the quadrupole error bound */
+void rb_set_theta_group(rb_sim* s, int on);     /* per-body theta, group-uniform (smallest) */
 
 int rb_bbox(rb_sim* s);
 int rb_build(rb_sim* s);

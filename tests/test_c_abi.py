@@ -37,8 +37,19 @@ def test_config_struct_layout_matches_header():
     assert cfg.abi_version == L.NBH_ABI_VERSION
     assert (cfg.theta, cfg.G, cfg.pool_factor) == (0.5, 1.0, 2.0)
     assert cfg.eps == pytest.approx(0.05) and cfg.dt == pytest.approx(0.025)
-    assert cfg.vote_width == 32 and cfg.arith == L.NBH_ARITH_FMA and cfg.use_graph == 1
+    assert cfg.vote_width == 64 and cfg.arith == L.NBH_ARITH_FMA and cfg.use_graph == 1
     assert C.sizeof(L.NbhConfig) == 4 * (2 + 7 + 5 + 8)
+
+
+def test_mlp_constants_match_header_and_network_shape():
+    """NBH_MLP_PARAMS = 12*64 + 64 + 64*64 + 64 + 64 + 1 (W1, b1, W2, b2, W3, b3), the same in
+    the header, the binding and the CPU reference of the network."""
+    import mlp_ref
+    src = open(HEADER).read()
+    hdr = int(re.search(r"#define NBH_MLP_PARAMS (\d+)", src).group(1))
+    feats = int(re.search(r"#define NBH_MLP_FEATURES (\d+)", src).group(1))
+    assert hdr == L.NBH_MLP_PARAMS == mlp_ref.NPARAMS == 12 * 64 + 64 + 64 * 64 + 64 + 64 + 1
+    assert feats == L.NBH_MLP_FEATURES == 12
 
 
 def test_number_of_nodes_matches_reference_formula():
@@ -65,7 +76,8 @@ def test_create_without_gpu_fails_loudly():
 
 
 def test_invalid_config_rejected():
-    for kw in ({"eps": 0.0}, {"vote_width": 8}, {"theta": -1.0}, {"pool_factor": 0.0}):
+    for kw in ({"eps": 0.0}, {"vote_width": 8}, {"vote_width": 128}, {"theta": -1.0}, {"pool_factor": 0.0},
+               {"vote_width": 64, "arith": L.NBH_ARITH_REFERENCE}):
         with pytest.raises(nbh.NbhError) as ei:
             nbh.Simulation(**kw)
         assert ei.value.code == L.NBH_ERR_INVALID, kw

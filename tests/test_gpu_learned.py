@@ -98,17 +98,20 @@ def test_bf16_inference_matches_reference():
     assert th.min() >= 0.3 - 1e-6 and th.max() <= 1.0 + 1e-6
 
 
-def test_per_body_theta_walk_matches_oracle():
+@pytest.mark.parametrize("vote,group", [(32, 0), (64, 0), (64, 1), (16, 1)])
+def test_per_body_theta_walk_matches_oracle(vote, group):
     from nbh import learned as LR
     n = 30000
     arrs = plummer(n, seed=5)
-    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=vote)
     g.load(*arrs)
+    LR.set_grouping(g, group)
     th = np.random.default_rng(7).uniform(0.35, 0.95, n).astype(np.float32)
     ax, ay, az, eb, inter = LR.probe(g, th)
-    o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=32, fma=True)
+    o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=vote, fma=True)
     o.load(*arrs)
     o.set_theta_body(th)
+    o.set_theta_group(group)
     o.enable_ebound()
     o.tree()
     o.force()

@@ -7,7 +7,8 @@ Two arithmetic modes are checked:
 * FMA mode (vote width 32, hardware rsqrt; the production path): same tree, same
   depth-first order and the same interaction count as the oracle; accelerations within
   relative 1e-4 per body (median 2e-6) of it, the difference being the ~2 ulp hardware
-  inverse square root.
+  inverse square root.  Vote width 64 (two bodies per lane) is checked the same way
+  against the oracle's 64-body groups.
 """
 import os
 
@@ -80,7 +81,7 @@ def test_fma_mode_matches_oracle_one_step():
     """16,384 bodies uniform in the unit ball, theta 0.5, eps 0.05, dt 0.025."""
     n = 16384
     arrs = ball(n, seed=5)
-    g = gpu_sim(theta=0.5, eps=0.05, dt=0.025)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.025, vote_width=32)
     g.load(*arrs)
     o = oracle_for(n, theta=0.5, eps=0.05, dt=0.025, vote=32, fma=True)
     o.load(*arrs)
@@ -103,7 +104,7 @@ def test_fma_mode_ten_steps_positions():
     1e-5 of the oracle's (relative to their extent)."""
     n = 16384
     arrs = ball(n, seed=6)
-    g = gpu_sim(theta=0.5, eps=0.05, dt=0.025)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.025, vote_width=32)
     g.load(*arrs)
     o = oracle_for(n, theta=0.5, eps=0.05, dt=0.025, vote=32, fma=True)
     o.load(*arrs)
@@ -121,7 +122,7 @@ def test_tree_matches_oracle_and_invariants():
     (same summation order)."""
     n = 20000
     arrs = plummer(n, seed=9)
-    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=32)
     g.load(*arrs)
     g.step()
     o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=32, fma=True)
@@ -154,7 +155,7 @@ def test_batch_of_universes_matches_oracle_per_universe():
     counts = [1024, 33, 5000, 1, 12000, 2048]
     parts = [U.PlummerUniverseGenerator(seed=40 + i).arrays(c) for i, c in enumerate(counts)]
     cat = [np.concatenate([p[k] for p in parts]) for k in range(7)]
-    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=32)
     g.load_batch(counts, *cat)
     g.step(3)
     gs = g.read()
@@ -175,6 +176,50 @@ def test_batch_of_universes_matches_oracle_per_universe():
         off += c
     assert g.stats()["interactions"] == total_inter
     assert isinstance(nbh.Simulation, type)
+
+
+@pytest.mark.parametrize("n", [20000, 64, 65, 1])
+def test_vote64_matches_oracle_one_step(n):
+    """Vote width 64 (two bodies per lane): groups of 64 consecutive sorted bodies, the
+    last one ragged; same interactions, same depth-first order, accelerations within the
+    FMA tolerance of the oracle's 64-body groups."""
+    arrs = plummer(n, seed=21)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=64)
+    g.load(*arrs)
+    o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=64, fma=True)
+    o.load(*arrs)
+    g.step(2)
+    o.step(2)
+    gs, os_ = g.read(), o.state()
+    st = g.stats()
+    assert st["interactions"] == o.interactions
+    np.testing.assert_array_equal(g.tree()["sorted"], o.tree_arrays()["sorted"])
+    rel, _ = acc_rel(gs, os_)
+    assert rel.max() <= FMA_ACC_REL_MAX, rel.max()
+    for k in ("x", "y", "z"):
+        assert np.abs(gs[k] - os_[k]).max() <= 1e-5 * max(1.0, np.abs(os_[k]).max())
+
+
+def test_vote64_batch_of_universes():
+    """Vote width 64 over uneven universes: items never straddle a universe boundary."""
+    from nbh import universe as U
+    counts = [1024, 33, 5000, 1, 64, 65, 127]
+    parts = [U.PlummerUniverseGenerator(seed=60 + i).arrays(c) for i, c in enumerate(counts)]
+    cat = [np.concatenate([p[k] for p in parts]) for k in range(7)]
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=64)
+    g.load_batch(counts, *cat)
+    g.step(2)
+    gs = g.read()
+    total, off = 0, 0
+    for i, c in enumerate(counts):
+        o = oracle_for(c, theta=0.5, eps=0.05, dt=0.01, vote=64, fma=True)
+        o.load(*parts[i])
+        o.step(2)
+        rel, _ = acc_rel({k: gs[k][off:off + c] for k in KEYS}, o.state())
+        assert rel.max() <= FMA_ACC_REL_MAX, (i, rel.max())
+        total += o.interactions
+        off += c
+    assert g.stats()["interactions"] == total
 
 
 def test_graph_and_eager_paths_identical():
@@ -198,7 +243,7 @@ def test_precise_mode_matches_oracle():
     """Kahan-compensated updates and FP64 root/extent, GPU vs oracle in the same mode."""
     n = 8192
     arrs = plummer(n, seed=12)
-    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, precise=True)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, precise=True, vote_width=32)
     g.load(*arrs)
     o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=32, fma=True, precise=True)
     o.load(*arrs)
