@@ -37,11 +37,14 @@ for _p in (os.path.join(ROOT, "gpu-nbody_gb300"), os.path.join(ROOT, "oracle")):
 
 METRIC = "ms/step at 1M bodies, plain vs learned-theta at equal p99 force error; Gint/s"
 DEFAULT_VOTE = 64                   # libnbh's default vote width (nbh_config_default)
+# Kernels in one fixed-angle step graph: bbox, build (3 insertion phases), link,
+# summarize, sort, force, integrate.
+GRAPH_LAUNCHES = 9
 FLOPS_PER_INTERACTION = 20          # 3 sub, 3 fma (d^2+eps^2), rsqrt, 3 mul, 3 fma, ~7 more
 HBM_FALLBACK_GBS = 6800.0
-# DRAM bytes (read + write) of one force launch on the 1,048,576-body Plummer workload,
-# from the ncu capture summarised in profiles/force_kernel_plummer1M.md.
-FORCE_TRAFFIC_BYTES_1M = 182_850_048 + 22_608_640
+# DRAM bytes (read + write) of one force launch (vote width 64) on the 1,048,576-body
+# Plummer workload, from the ncu capture summarised in profiles/force_kernel_plummer1M.md.
+FORCE_TRAFFIC_BYTES_1M = 211_056_640 + 25_430_016
 
 # Algorithmic bytes per body / per cell of the memory-bound stages (minimum traffic:
 # every byte read and written once).
@@ -392,7 +395,8 @@ def main():
     achieved = FLOPS_PER_INTERACTION * inter_ts / (force_ms * 1e-3) / 1e12
     roofline = {"bound": "fp32", "kernel": "force_kernel<%d,FMA>" % args.vote_width, "achieved": achieved,
                 "peak": fp32.value, "unit": "TFLOP/s", "frac": achieved / fp32.value,
-                "traffic": FORCE_TRAFFIC_BYTES_1M if (args.workload == "plummer" and n == 1 << 20) else None,
+                "traffic": FORCE_TRAFFIC_BYTES_1M if (args.workload == "plummer" and n == 1 << 20
+                                                      and args.vote_width == DEFAULT_VOTE) else None,
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
                                   "(profiles/force_kernel_plummer1M.md)",
                 "flops_per_interaction": FLOPS_PER_INTERACTION,
@@ -486,7 +490,7 @@ def main():
             "e2e": {"value": e2e_ms / world, "unit": "ms/step", "h2d_bytes_per_step": 36 * n,
                     "d2h_bytes_per_step": 36 * n, "wall_ms_per_step": wall_ms,
                     "path": "nbh_write (pinned host) -> nbh_step -> nbh_read (pinned host)"},
-            "gpu_launches": 6 * args.steps,
+            "gpu_launches": GRAPH_LAUNCHES * args.steps,
             "clocks": clock_info,
             "cpu_baseline": cpu,
             "learned_theta": learned,
