@@ -283,6 +283,7 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch geometry")
     ap.add_argument("--error-samples", type=int, default=4096)
     ap.add_argument("--profile-only", action="store_true",
                     help="load, warm up and run the timed steps only (for ncu captures)")
@@ -346,6 +347,9 @@ def main():
     for _ in range(args.warmup):
         flush_l2(stream)
         sim.step(1)
+    # launch geometry picked by the library's autotuner (changes no result); profile runs
+    # keep the default geometry so that their launch lists hold only the step's kernels
+    tune = None if (args.no_autotune or args.profile_only) else sim.autotune()
     force_error = None if args.profile_only else _step_error(sim, idx, O, np)
     clocks = ClockSampler(local) if rank == 0 else None
     if clocks:
@@ -366,7 +370,9 @@ def main():
 
     # per-stage device times (eager launches with events between stages)
     hbm_peak, peak_src = _peaks()
-    ts = new_sim(stage_timing=True)
+    geometry = {} if tune is None else {"force_threads": tune["force_threads"], "stack_cap": tune["stack_cap"],
+                                        "build_phases": tune["build_phases"]}
+    ts = new_sim(stage_timing=True, **geometry)
     ts.step(2)
     tstream = torch.cuda.ExternalStream(ts.stream, device=dev)
     acc = {k: 0.0 for k in ("ms_bbox", "ms_build", "ms_summarize", "ms_sort", "ms_force", "ms_integrate", "ms_step")}
@@ -437,7 +443,7 @@ def main():
     model_path = LR.default_model_path()
     if not args.no_learned and os.path.exists(model_path):
         model = LR.load_model(model_path)
-        ls = new_sim()
+        ls = new_sim(**geometry)
         LR.install(ls, model)
         lstream = torch.cuda.ExternalStream(ls.stream, device=dev)
         for _ in range(args.warmup):
@@ -487,6 +493,9 @@ def main():
             "stage_ms": {k[3:]: v for k, v in acc.items()},
             "stages": stages,
             "roofline": roofline,
+            "autotune": None if tune is None else {k: tune[k] for k in (
+                "force_threads", "stack_cap", "build_phases", "max_depth", "ms_force", "ms_force_before",
+                "ms_tree", "ms_tree_before")},
             "e2e": {"value": e2e_ms / world, "unit": "ms/step", "h2d_bytes_per_step": 36 * n,
                     "d2h_bytes_per_step": 36 * n, "wall_ms_per_step": wall_ms,
                     "path": "nbh_write (pinned host) -> nbh_step -> nbh_read (pinned host)"},

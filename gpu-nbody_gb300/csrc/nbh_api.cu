@@ -47,6 +47,9 @@ struct nbh_sim {
     bool theta_active = false;     // learned opening angle on
     int theta_every = 1;           // steps between evaluations of the model
     int theta_group = 0;           // 1: each vote group walks with its smallest angle
+    int force_threads = 128;       // force launch geometry (nbh_autotune)
+    int stack_cap = 256;
+    int build_phases = 3;          // octree insertion launches
     ThetaDev* model = nullptr;     // installed model (device)
     float* model_prm = nullptr;    // its FP32 parameters (device)
     float* probe_theta = nullptr;  // per-body theta of the last force probe (device)
@@ -146,6 +149,7 @@ StepParams step_params(const nbh_sim* sim) {
     p.sorted = sim->sorted;
     p.theta_body = sim->theta_active ? sim->theta_body : nullptr;
     p.theta_group = sim->theta_group;
+    p.stack_cap = sim->stack_cap;
     p.st = sim->st;
     p.ubody = sim->ubody;
     p.ubox = sim->ubox;
@@ -176,7 +180,7 @@ void enqueue_step(nbh_sim* sim, bool timed) {
     if (timed) cudaEventRecord(sim->ev[0], s);
     launch_bbox(p, sim->grid_bbox, s);
     if (timed) cudaEventRecord(sim->ev[1], s);
-    launch_build(p, s);
+    launch_build(p, sim->build_phases, s);
     launch_link(p, sim->grid_sum, s);
     if (timed) cudaEventRecord(sim->ev[2], s);
     launch_summarize(p, ref, sim->grid_sum, s);
@@ -187,11 +191,11 @@ void enqueue_step(nbh_sim* sim, bool timed) {
     if (sim->theta_active && sim->theta_every > 1) {
         StepParams pg = p;
         pg.feat_gate = 1;    // the walk before an evaluation records the error bounds
-        launch_force(pg, sim->cfg.vote_width, ref, true, sim->grid_force, s);
+        launch_force(pg, sim->cfg.vote_width, ref, true, sim->grid_force, sim->force_threads, s);
         pg.feat_gate = 2;
-        launch_force(pg, sim->cfg.vote_width, ref, false, sim->grid_force, s);
+        launch_force(pg, sim->cfg.vote_width, ref, false, sim->grid_force, sim->force_threads, s);
     } else {
-        launch_force(p, sim->cfg.vote_width, ref, sim->theta_active, sim->grid_force, s);
+        launch_force(p, sim->cfg.vote_width, ref, sim->theta_active, sim->grid_force, sim->force_threads, s);
     }
     if (timed) cudaEventRecord(sim->ev[5], s);
     launch_integrate(p, ref, sim->grid_int, s);
@@ -204,7 +208,7 @@ void enqueue_tree(nbh_sim* sim, const StepParams& p) {
     const bool ref = sim->cfg.arith == NBH_ARITH_REFERENCE;
     cudaStream_t s = sim->stream;
     launch_bbox(p, sim->grid_bbox, s);
-    launch_build(p, s);
+    launch_build(p, sim->build_phases, s);
     launch_link(p, sim->grid_sum, s);
     launch_summarize(p, ref, sim->grid_sum, s);
     launch_sort(p, sim->grid_sort, s);
@@ -239,7 +243,7 @@ int set_geometry(nbh_sim* sim) {
     int occ_sort = 0, occ_force = 0;
     CK(static_cast<cudaError_t>(occupancy_sort(&occ_sort)));
     CK(static_cast<cudaError_t>(occupancy_force(sim->cfg.vote_width, sim->cfg.arith == NBH_ARITH_REFERENCE,
-                                                &occ_force)));
+                                                sim->force_threads, sim->stack_cap, &occ_force)));
     sim->grid_bbox = std::max(1, std::min(sim->nchunks, 4 * sms));
     sim->grid_sum = std::max(1, (sim->nbody + 255) / 256);
     sim->grid_sort = std::max(1, std::min(occ_sort * sms, (sim->ncells + 255) / 256));
@@ -453,6 +457,13 @@ int nbh_create(const nbh_config* cfg_in, nbh_sim** out) {
         return fail(nullptr, NBH_ERR_INVALID, "vote_width 64 takes FMA arithmetic");
     if (cfg.arith != NBH_ARITH_FMA && cfg.arith != NBH_ARITH_REFERENCE)
         return fail(nullptr, NBH_ERR_INVALID, "arith must be NBH_ARITH_FMA or NBH_ARITH_REFERENCE");
+    const int threads = cfg.force_threads ? cfg.force_threads : 128;
+    const int cap = cfg.stack_cap ? cfg.stack_cap : 256;
+    if (!force_geometry_valid(cfg.vote_width, threads, cap))
+        return fail(nullptr, NBH_ERR_INVALID, "force_threads must be 64, 128 or 256 and stack_cap a multiple of 8 "
+                                              "in [64, 256]");
+    if (cfg.build_phases != 0 && cfg.build_phases != 1 && cfg.build_phases != 3)
+        return fail(nullptr, NBH_ERR_INVALID, "build_phases must be 1 or 3");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0) return fail(nullptr, NBH_ERR_NODEVICE, "no CUDA device");
@@ -466,6 +477,9 @@ int nbh_create(const nbh_config* cfg_in, nbh_sim** out) {
     sim->err.reserve(1024);   // error messages of later calls then fit without allocating
     sim->cfg = cfg;
     sim->device = cfg.device;
+    sim->force_threads = threads;
+    sim->stack_cap = cap;
+    sim->build_phases = cfg.build_phases ? cfg.build_phases : 3;
     sim->sms = prop.multiProcessorCount;
     if ((e = cudaSetDevice(cfg.device)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&sim->stream, cudaStreamNonBlocking)) != cudaSuccess ||
@@ -839,6 +853,196 @@ int nbh_direct_f64(nbh_sim* sim, int32_t nidx, const int32_t* idx, double* ax, d
     return NBH_OK;
 }
 
+int nbh_diagnostics(nbh_sim* sim, int32_t flags, nbh_diag* out, int32_t nout) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_diagnostics before nbh_load");
+    if (nout < 0 || (nout > 0 && !out) || (flags & ~NBH_DIAG_POTENTIAL))
+        return fail(sim, NBH_ERR_INVALID, "bad arguments");
+    const bool potential = (flags & NBH_DIAG_POTENTIAL) != 0;
+    CK(cudaSetDevice(sim->device));
+    cudaStream_t s = sim->stream;
+    double* d_part = nullptr;
+    double* d_out = nullptr;
+    cudaError_t e;
+    if ((e = cudaMallocAsync(reinterpret_cast<void**>(&d_part), sizeof(double) * kDiagFields * sim->nchunks, s)) !=
+            cudaSuccess ||
+        (e = cudaMallocAsync(reinterpret_cast<void**>(&d_out), sizeof(double) * kDiagFields * sim->nuniv, s)) !=
+            cudaSuccess) {
+        if (d_part) cudaFreeAsync(d_part, s);
+        return cuda_fail(sim, "cudaMallocAsync", e);
+    }
+    const nbh_config& c = sim->cfg;
+    const float eps2f = c.eps2 > 0.0f ? c.eps2 : c.eps * c.eps;
+    launch_diagnostics(sim->node4, sim->vel, sim->chunks, sim->nchunks, sim->ubody, sim->nuniv, potential, eps2f,
+                       d_part, d_out, s);
+    std::vector<double> h((size_t)kDiagFields * sim->nuniv);
+    cudaMemcpyAsync(h.data(), d_out, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d_part, s);
+    cudaFreeAsync(d_out, s);
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+    const int nfill = std::min(nout, sim->nuniv);
+    const double G = c.G;
+    for (int u = 0; u < nfill; ++u) {
+        const double* r = h.data() + (size_t)kDiagFields * u;
+        nbh_diag& d = out[u];
+        d.mass = r[0];
+        for (int k = 0; k < 3; ++k) {
+            d.com[k] = r[0] > 0.0 ? r[1 + k] / r[0] : 0.0;
+            d.momentum[k] = r[4 + k];
+            d.angular_momentum[k] = r[7 + k];
+        }
+        d.kinetic = r[10];
+        // each pair appears in both bodies' sums
+        d.potential = potential ? 0.5 * G * r[11] : 0.0;
+        d.potential_unsoftened = potential ? 0.5 * G * r[12] : 0.0;
+        d.max_depth = sim->h_state->max_depth;
+        d.has_potential = potential ? 1 : 0;
+    }
+    return nfill;
+}
+
+int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
+    if (!sim || !out) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_autotune before nbh_load");
+    if (flags != 0) return fail(sim, NBH_ERR_INVALID, "flags must be 0");
+    CK(cudaSetDevice(sim->device));
+    cudaStream_t s = sim->stream;
+    std::memset(out, 0, sizeof(*out));
+    const bool ref = sim->cfg.arith == NBH_ARITH_REFERENCE;
+    const int vote = sim->cfg.vote_width;
+    // snapshot of the device state word: restored at the end, so the step counter, the
+    // depth and the counters read as before
+    DevState saved;
+    CK(cudaMemcpyAsync(&saved, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (saved.status != NBH_OK) return fail(sim, NBH_ERR_STATE, "nbh_autotune after a failed step");
+    int e;
+    {
+        StepParams p = step_params(sim);
+        p.theta_body = nullptr;
+        if ((e = rebuild_tree(sim, p))) return e;
+    }
+    const int depth = sim->h_state->max_depth;
+    out->max_depth = depth;
+    cudaEvent_t a = nullptr, b = nullptr;
+    CK(cudaEventCreate(&a));
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return fail(sim, NBH_ERR_CUDA, "cudaEventCreate");
+    }
+    auto timed = [&](auto&& launch, float* ms) -> cudaError_t {
+        float tot = 0.0f;
+        for (int r = 0; r < 4; ++r) {                 // one warm-up, three timed
+            cudaMemsetAsync(&sim->st->force_next, 0, sizeof(int), s);
+            cudaMemsetAsync(&sim->st->interactions, 0, sizeof(unsigned long long), s);
+            cudaEventRecord(a, s);
+            launch();
+            cudaEventRecord(b, s);
+            cudaError_t err = cudaStreamSynchronize(s);
+            if (err != cudaSuccess) return err;
+            float t = 0.0f;
+            cudaEventElapsedTime(&t, a, b);
+            if (r) tot += t;
+        }
+        *ms = tot / 3.0f;
+        return cudaGetLastError();
+    };
+    auto add_trial = [&](int kind, int x, int y, float ms) {
+        if (out->trials < NBH_TUNE_MAX_TRIALS) {
+            out->trial_kind[out->trials] = kind;
+            out->trial_a[out->trials] = x;
+            out->trial_b[out->trials] = y;
+            out->trial_ms[out->trials] = ms;
+            ++out->trials;
+        }
+    };
+    // force geometries: stacks from the smallest that walks this depth (+2 levels of
+    // headroom) on the fast path, to the largest; the geometry in place is always timed
+    int cap_fit = 7 * (depth + 1) + 8;
+    cap_fit = std::max(64, (cap_fit + 7) / 8 * 8);
+    std::vector<std::pair<int, int>> geo;
+    const int threads_c[3] = {64, 128, 256};
+    for (int t : threads_c) {
+        if (cap_fit <= 256) {
+            geo.push_back({t, cap_fit});
+            const int mid = ((cap_fit + 256) / 2 + 7) / 8 * 8;
+            if (mid != cap_fit && mid != 256) geo.push_back({t, mid});
+        }
+        geo.push_back({t, 256});
+    }
+    geo.push_back({sim->force_threads, sim->stack_cap});
+    std::sort(geo.begin(), geo.end());
+    geo.erase(std::unique(geo.begin(), geo.end()), geo.end());
+    float best_ms = 1e30f;
+    int best_t = sim->force_threads, best_c = sim->stack_cap;
+    cudaError_t err = cudaSuccess;
+    for (const auto& g : geo) {
+        if (!force_geometry_valid(vote, g.first, g.second)) continue;
+        int occ = 0;
+        if ((err = static_cast<cudaError_t>(occupancy_force(vote, ref, g.first, g.second, &occ))) != cudaSuccess) break;
+        if (occ < 1) continue;
+        StepParams q = step_params(sim);
+        q.theta_body = nullptr;
+        q.probe = sim->probe;           // results go to the scratch buffer, body state untouched
+        q.stack_cap = g.second;
+        const int grid = occ * sim->sms;
+        float ms = 0.0f;
+        err = timed([&] { launch_force(q, vote, ref, false, grid, g.first, s); }, &ms);
+        if (err != cudaSuccess) break;
+        add_trial(0, g.first, g.second, ms);
+        if (g.first == sim->force_threads && g.second == sim->stack_cap) out->ms_force_before = ms;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best_t = g.first;
+            best_c = g.second;
+        }
+    }
+    // tree stages with one and three insertion phases
+    const int phases_before = sim->build_phases;
+    float best_tree = 1e30f;
+    int best_ph = phases_before;
+    const int phase_c[2] = {1, 3};
+    for (int ph : phase_c) {
+        if (err != cudaSuccess) break;
+        sim->build_phases = ph;
+        StepParams p = step_params(sim);
+        p.theta_body = nullptr;
+        float ms = 0.0f;
+        err = timed([&] { enqueue_tree(sim, p); }, &ms);
+        if (err != cudaSuccess) break;
+        add_trial(1, ph, 0, ms);
+        if (ph == phases_before) out->ms_tree_before = ms;
+        if (ms < best_tree) {
+            best_tree = ms;
+            best_ph = ph;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    sim->build_phases = phases_before;
+    if (err != cudaSuccess) return cuda_fail(sim, "nbh_autotune", err);
+    CK(cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (sim->h_state->status != NBH_OK) return fail(sim, sim->h_state->status, "nbh_autotune: a timed launch failed");
+    // the state word as it was (the tree is rebuilt by the next step in any case)
+    *sim->h_state = saved;
+    CK(cudaMemcpyAsync(sim->st, sim->h_state, sizeof(DevState), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    sim->force_threads = best_t;
+    sim->stack_cap = best_c;
+    sim->build_phases = best_ph;
+    if ((e = set_geometry(sim))) return e;
+    drop_graph(sim);
+    out->force_threads = best_t;
+    out->stack_cap = best_c;
+    out->build_phases = best_ph;
+    out->ms_force = best_ms;
+    out->ms_tree = best_tree;
+    return NBH_OK;
+}
+
 int nbh_direct_f64_static(nbh_sim* sim, int32_t nidx, const int32_t* idx, double* ax, double* ay, double* az) {
     if (!sim) return NBH_ERR_INVALID;
     if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_direct_f64_static before nbh_load");
@@ -996,7 +1200,8 @@ int nbh_force_probe(nbh_sim* sim, const float* theta_body, float* ax, float* ay,
     const unsigned long long z64 = 0;
     CK(cudaMemcpyAsync(&sim->st->force_next, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(&sim->st->interactions, &z64, sizeof(z64), cudaMemcpyHostToDevice, s));
-    launch_force(p, sim->cfg.vote_width, sim->cfg.arith == NBH_ARITH_REFERENCE, true, sim->grid_force, s);
+    launch_force(p, sim->cfg.vote_width, sim->cfg.arith == NBH_ARITH_REFERENCE, true, sim->grid_force,
+                 sim->force_threads, s);
     CK(cudaGetLastError());
     std::vector<float4> out((size_t)n);
     CK(cudaMemcpyAsync(out.data(), sim->probe, sizeof(float4) * n, cudaMemcpyDeviceToHost, s));

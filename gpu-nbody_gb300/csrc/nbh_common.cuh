@@ -99,6 +99,7 @@ struct StepParams {
     float dt;
     float G;
     int precise;
+    int stack_cap;       // entries of each force group's shared-memory stack
     int theta_group;     // per-body theta: 1 = each vote group walks with its smallest angle
     int feat_gate;       // force launch gated on the learned-theta schedule: 0 none,
                          // 1 run only on bound-recording steps, 2 only on the others

@@ -4,13 +4,15 @@
 
 namespace nbh {
 
-constexpr int kForceThreads = 128;
-// Per-group stack of pending children, each with its preloaded node record.  Opening a
-// cell at level l while every ancestor still has 7 pending children needs 7*l + 8
-// entries, so kStackCap entries cover trees up to kFastMaxDepth levels; deeper trees (or
-// pools beyond kFastMaxNodes) take the per-level (cell, next child) walk.
-constexpr int kStackCap = 256;
-constexpr int kFastMaxDepth = (kStackCap - 8) / 7 + 1;
+// Launch geometry is chosen at run time (nbh_autotune): threads per block (64 / 128 / 256)
+// and the entries of each group's shared-memory stack of pending children, each with its
+// preloaded node record.  Opening a cell at level l while every ancestor still has 7
+// pending children needs 7*l + 8 entries, so a stack of `cap` entries covers trees up to
+// fast_max_depth(cap) levels; deeper trees take the per-level (cell, next child) walk.
+constexpr int kForceThreadsMax = 256;
+constexpr int kStackCapMax = 256;
+constexpr int kStackCapMin = 64;     // the deep walk keeps 2 * kMaxDepth ints in the same space
+__host__ __device__ constexpr int fast_max_depth(int cap) { return (cap - 8) / 7 + 1; }
 
 // Lanes of one vote group: W bodies on W lanes for W <= 32; W = 64 puts two bodies on
 // each lane of one warp.
@@ -20,8 +22,8 @@ __host__ __device__ constexpr int group_lanes() {
 }
 
 template <int W>
-constexpr size_t force_smem_bytes() {
-    return (size_t)(kForceThreads / group_lanes<W>()) * kStackCap * (sizeof(float4) + sizeof(int2));
+constexpr size_t force_smem_bytes(int threads, int cap) {
+    return (size_t)(threads / group_lanes<W>()) * cap * (sizeof(float4) + sizeof(int2));
 }
 
 // Opening threshold of tree level L (root = 0): r^2/theta^2 * 4^-L + eps^2
@@ -96,30 +98,31 @@ __device__ __forceinline__ float dist2(const float dx, const float dy, const flo
 // p.feat_gate set, a launch that does not match the step's place in the learned-theta
 // schedule returns at once (the step graph holds a recording and a plain launch).
 template <int W, bool REF, bool PB, bool FEAT>
-__global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
+__global__ void __launch_bounds__(kForceThreadsMax) force_kernel(StepParams p) {
     if (load_status(p.st)) return;
     if (p.feat_gate && theta_bound_step(p.st, p.st->step) != (p.feat_gate == 1)) return;
     constexpr int GL = group_lanes<W>();            // lanes per group
     constexpr int BPL = W / GL;                     // bodies per lane
-    constexpr int kGroups = kForceThreads / GL;
+    const int cap = p.stack_cap;
+    const int groups = blockDim.x / GL;
     // The stack entry carries the finished threshold when it is the same for every body
     // of the group (fixed angle) and nothing else needs the level factor.
     constexpr bool kStoreDq = !PB && !FEAT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float4* const sq_all = reinterpret_cast<float4*>(smem_raw);
-    int2* const se_all = reinterpret_cast<int2*>(sq_all + kGroups * kStackCap);
+    int2* const se_all = reinterpret_cast<int2*>(sq_all + groups * cap);
     const int lane = threadIdx.x & 31;
     const int grp = threadIdx.x / GL;
     const int glane = threadIdx.x % GL;
     const unsigned gmask = (GL == 32) ? 0xffffffffu : (0xffffu << (16 * (lane >> 4)));
-    float4* const sq = sq_all + grp * kStackCap;     // node record of each pending child
-    int2* const se = se_all + grp * kStackCap;       // (node index, bits of threshold or level factor)
+    float4* const sq = sq_all + grp * cap;           // node record of each pending child
+    int2* const se = se_all + grp * cap;             // (node index, bits of threshold or level factor)
     int* const snode = reinterpret_cast<int*>(se);   // deep-tree walk: (cell, next) per level
     int* const snext = snode + kMaxDepth;
     const int nbody = p.nbody;
     const float eps2 = p.eps2;
     const int step = p.st->step;
-    const bool fast = p.st->max_depth <= kFastMaxDepth;
+    const bool fast = p.st->max_depth <= fast_max_depth(cap);
     const float4* __restrict__ node4 = p.node4;
     const int* __restrict__ child = p.child;
     const float4* __restrict__ kids4 = p.kids4;
@@ -200,7 +203,7 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
                     }
                     const unsigned bal = __ballot_sync(gmask, glane < 8 && chk >= 0) & gmask;
                     const int cnt = __popc(bal);
-                    if (top + cnt > kStackCap) {           // unreachable below kFastMaxDepth
+                    if (top + cnt > cap) {                 // unreachable below fast_max_depth(cap)
                         raise_error(p.st, NBH_ERR_DEPTH);
                         ok = false;
                         break;
@@ -348,22 +351,23 @@ __global__ void __launch_bounds__(kForceThreads) force_kernel(StepParams p) {
 
 // -------------------------------------------------------------------------------------
 template <int W, bool REF, bool PB>
-static void launch_force_pf(const StepParams& p, bool feat, int grid, cudaStream_t s) {
-    constexpr size_t sm = force_smem_bytes<W>();
-    if (feat) force_kernel<W, REF, PB, true><<<grid, kForceThreads, sm, s>>>(p);
-    else force_kernel<W, REF, PB, false><<<grid, kForceThreads, sm, s>>>(p);
+static void launch_force_pf(const StepParams& p, bool feat, int grid, int threads, cudaStream_t s) {
+    const size_t sm = force_smem_bytes<W>(threads, p.stack_cap);
+    if (feat) force_kernel<W, REF, PB, true><<<grid, threads, sm, s>>>(p);
+    else force_kernel<W, REF, PB, false><<<grid, threads, sm, s>>>(p);
 }
 
 template <int W, bool REF>
-static void launch_force_t(const StepParams& p, bool pb, bool feat, int grid, cudaStream_t s) {
-    if (pb) launch_force_pf<W, REF, true>(p, feat, grid, s);
-    else launch_force_pf<W, REF, false>(p, feat, grid, s);
+static void launch_force_t(const StepParams& p, bool pb, bool feat, int grid, int threads, cudaStream_t s) {
+    if (pb) launch_force_pf<W, REF, true>(p, feat, grid, threads, s);
+    else launch_force_pf<W, REF, false>(p, feat, grid, threads, s);
 }
 
+// Every variant may be launched with up to the largest geometry's shared memory.
 template <int W, bool REF, bool PB, bool FEAT>
 static cudaError_t prep_force() {
     return cudaFuncSetAttribute(force_kernel<W, REF, PB, FEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)force_smem_bytes<W>());
+                                (int)force_smem_bytes<W>(kForceThreadsMax, kStackCapMax));
 }
 
 template <int W, bool REF>
@@ -386,29 +390,42 @@ int prepare_force_kernels() {
     return (int)e;
 }
 
-void launch_force(const StepParams& p, int vote, bool ref, bool feat, int grid, cudaStream_t s) {
+bool force_geometry_valid(int vote, int threads, int cap) {
+    const int gl = vote < 32 ? vote : 32;
+    return (threads == 64 || threads == 128 || threads == 256) && threads % gl == 0 && cap >= kStackCapMin &&
+           cap <= kStackCapMax && cap % 8 == 0;
+}
+
+int force_fast_max_depth(int cap) { return fast_max_depth(cap); }
+
+void launch_force(const StepParams& p, int vote, bool ref, bool feat, int grid, int threads, cudaStream_t s) {
     const bool pb = p.theta_body != nullptr;
     if (vote == 64) {
-        launch_force_t<64, false>(p, pb, feat, grid, s);   // FMA arithmetic only
+        launch_force_t<64, false>(p, pb, feat, grid, threads, s);   // FMA arithmetic only
     } else if (vote == 16) {
-        if (ref) launch_force_t<16, true>(p, pb, feat, grid, s);
-        else launch_force_t<16, false>(p, pb, feat, grid, s);
+        if (ref) launch_force_t<16, true>(p, pb, feat, grid, threads, s);
+        else launch_force_t<16, false>(p, pb, feat, grid, threads, s);
     } else {
-        if (ref) launch_force_t<32, true>(p, pb, feat, grid, s);
-        else launch_force_t<32, false>(p, pb, feat, grid, s);
+        if (ref) launch_force_t<32, true>(p, pb, feat, grid, threads, s);
+        else launch_force_t<32, false>(p, pb, feat, grid, threads, s);
     }
 }
 
-int occupancy_force(int vote, bool ref, int* blocks_per_sm) {
-    const size_t s16 = force_smem_bytes<16>(), s32 = force_smem_bytes<32>(), s64 = force_smem_bytes<64>();
+// Resident blocks per SM of the fixed-angle variant at this geometry (the per-body
+// variants use as many registers or fewer per resident warp budget; their grid is the same).
+int occupancy_force(int vote, bool ref, int threads, int cap, int* blocks_per_sm) {
     if (vote == 64)
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<64, false, false, false>,
-                                                             kForceThreads, s64);
+                                                             threads, force_smem_bytes<64>(threads, cap));
     if (vote == 16)
-        return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, true, false, false>, kForceThreads, s16)
-                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, false, false, false>, kForceThreads, s16);
-    return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<32, true, false, false>, kForceThreads, s32)
-               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<32, false, false, false>, kForceThreads, s32);
+        return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, true, false, false>,
+                                                                   threads, force_smem_bytes<16>(threads, cap))
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, false, false, false>,
+                                                                   threads, force_smem_bytes<16>(threads, cap));
+    return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<32, true, false, false>,
+                                                               threads, force_smem_bytes<32>(threads, cap))
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<32, false, false, false>,
+                                                               threads, force_smem_bytes<32>(threads, cap));
 }
 
 }  // namespace nbh

@@ -7,11 +7,13 @@ namespace nbh {
 struct StepParams;
 
 void launch_bbox(const StepParams& p, int grid, cudaStream_t s);
-void launch_build(const StepParams& p, cudaStream_t s);
+void launch_build(const StepParams& p, int phases, cudaStream_t s);   // 1 or 3 insertion phases
 void launch_link(const StepParams& p, int grid, cudaStream_t s);
 void launch_summarize(const StepParams& p, bool ref, int grid, cudaStream_t s);
 void launch_sort(const StepParams& p, int grid, cudaStream_t s);
-void launch_force(const StepParams& p, int vote, bool ref, bool feat, int grid, cudaStream_t s);
+void launch_force(const StepParams& p, int vote, bool ref, bool feat, int grid, int threads, cudaStream_t s);
+bool force_geometry_valid(int vote, int threads, int cap);
+int force_fast_max_depth(int cap);   // deepest tree the stack of `cap` entries walks without the per-level walk
 void launch_integrate(const StepParams& p, bool ref, int grid, cudaStream_t s);
 
 void launch_pack(int n, const float* soa, int mask, float4* node4, float4* vel, float4* acc, int grid,
@@ -23,12 +25,19 @@ void launch_export4(int n, const float4* node4, const float4* vel, float4* pos4,
 void launch_direct_f64(const float4* node4, int nidx, const int* idx, const int2* range, double eps2, double G,
                        double* out, int ysplit, cudaStream_t s);
 
+// Diagnostics rows (nbh_diag.cu): 0 mass, 1-3 m x, 4-6 m v, 7-9 m x cross v, 10 kinetic
+// energy, 11 / 12 sum_i m_i phi_i softened / unsoftened (each pair twice).
+constexpr int kDiagMoments = 11;
+constexpr int kDiagFields = 13;
+void launch_diagnostics(const float4* node4, const float4* vel, const int4* chunks, int nchunks, const int* ubody,
+                        int nuniv, bool potential, float eps2, double* part, double* out, cudaStream_t s);
+
 struct DevState;
 void launch_wait_selftest(const int* flag, unsigned long long limit_ns, DevState* st, cudaStream_t s);
 void launch_fma_peak(float* sink, int iters, int grid, int block, cudaStream_t s);
 
 int occupancy_sort(int* blocks_per_sm);
-int occupancy_force(int vote, bool ref, int* blocks_per_sm);
+int occupancy_force(int vote, bool ref, int threads, int cap, int* blocks_per_sm);
 int prepare_force_kernels();   // raises the dynamic shared-memory limit of the force kernels
 
 }  // namespace nbh

@@ -139,11 +139,12 @@ __global__ void __launch_bounds__(256) bbox_kernel(StepParams p) {
 // descents spread over many cells and rarely meet a locked slot.
 constexpr int kBuildPhases = 3;
 __host__ __device__ constexpr int phase_bodies(int phase) {   // per full 256-body chunk
-    return phase == 0 ? 1 : (phase == 1 ? 15 : 240);
+    return phase < 0 ? 256 : (phase == 0 ? 1 : (phase == 1 ? 15 : 240));
 }
 // Offset inside its chunk of the phase's idx-th body: 0; 16, 32, ..., 240; the rest.
+// Phase -1 is a single pass over every body.
 __device__ __forceinline__ int phase_offset(int phase, int idx) {
-    return phase == 0 ? 0 : (phase == 1 ? 16 * (idx + 1) : idx + idx / 15 + 1);
+    return phase < 0 ? idx : (phase == 0 ? 0 : (phase == 1 ? 16 * (idx + 1) : idx + idx / 15 + 1));
 }
 
 __global__ void __launch_bounds__(256) build_kernel(StepParams p, int phase) {
@@ -441,7 +442,12 @@ void launch_bbox(const StepParams& p, int grid, cudaStream_t s) {
     if (p.precise) bbox_kernel<true><<<grid, 256, 0, s>>>(p);
     else bbox_kernel<false><<<grid, 256, 0, s>>>(p);
 }
-void launch_build(const StepParams& p, cudaStream_t s) {
+void launch_build(const StepParams& p, int phases, cudaStream_t s) {
+    if (phases == 1) {      // a single pass over every body (phase index -1)
+        const long long bodies = (long long)p.nchunks * 256;
+        build_kernel<<<(unsigned)((bodies + 255) / 256), 256, 0, s>>>(p, -1);
+        return;
+    }
     for (int phase = 0; phase < kBuildPhases; ++phase) {
         const long long bodies = (long long)p.nchunks * phase_bodies(phase);
         build_kernel<<<(unsigned)((bodies + 255) / 256), 256, 0, s>>>(p, phase);

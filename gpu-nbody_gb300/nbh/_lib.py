@@ -43,7 +43,8 @@ class NbhConfig(C.Structure):
         ("theta", C.c_float), ("eps", C.c_float), ("theta2", C.c_float), ("eps2", C.c_float),
         ("dt", C.c_float), ("G", C.c_float), ("pool_factor", C.c_float),
         ("vote_width", C.c_int32), ("arith", C.c_int32), ("precise", C.c_int32),
-        ("stage_timing", C.c_int32), ("use_graph", C.c_int32), ("reserved", C.c_int32 * 8),
+        ("stage_timing", C.c_int32), ("use_graph", C.c_int32), ("force_threads", C.c_int32),
+        ("stack_cap", C.c_int32), ("build_phases", C.c_int32), ("reserved", C.c_int32 * 5),
     ]
 
 
@@ -58,6 +59,27 @@ class NbhStats(C.Structure):
         ("ms_step", C.c_float), ("reserved", C.c_float * 8),
     ]
 
+
+class NbhDiag(C.Structure):
+    _fields_ = [
+        ("mass", C.c_double), ("com", C.c_double * 3), ("momentum", C.c_double * 3),
+        ("angular_momentum", C.c_double * 3), ("kinetic", C.c_double), ("potential", C.c_double),
+        ("potential_unsoftened", C.c_double), ("max_depth", C.c_int32), ("has_potential", C.c_int32),
+    ]
+
+
+NBH_DIAG_POTENTIAL = 1
+NBH_TUNE_MAX_TRIALS = 16
+
+
+class NbhTune(C.Structure):
+    _fields_ = [
+        ("force_threads", C.c_int32), ("stack_cap", C.c_int32), ("build_phases", C.c_int32),
+        ("max_depth", C.c_int32), ("ms_force", C.c_float), ("ms_force_before", C.c_float),
+        ("ms_tree", C.c_float), ("ms_tree_before", C.c_float), ("trials", C.c_int32),
+        ("trial_kind", C.c_int32 * NBH_TUNE_MAX_TRIALS), ("trial_a", C.c_int32 * NBH_TUNE_MAX_TRIALS),
+        ("trial_b", C.c_int32 * NBH_TUNE_MAX_TRIALS), ("trial_ms", C.c_float * NBH_TUNE_MAX_TRIALS),
+    ]
 
 _P = C.c_void_p
 _F = C.POINTER(C.c_float)
@@ -88,6 +110,8 @@ SIGNATURES = {
     "nbh_read_tree": (C.c_int, [_P] + [_P] * 8),
     "nbh_direct_f64": (C.c_int, [_P, C.c_int32, _P, _P, _P, _P]),
     "nbh_direct_f64_static": (C.c_int, [_P, C.c_int32, _P, _P, _P, _P]),
+    "nbh_diagnostics": (C.c_int, [_P, C.c_int32, C.POINTER(NbhDiag), C.c_int32]),
+    "nbh_autotune": (C.c_int, [_P, C.c_int32, C.POINTER(NbhTune)]),
     "nbh_generate_uniform_ball": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_float, C.c_float] + [_P] * 7),
     "nbh_generate_plummer": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_float, C.c_float] + [_P] * 7),
     "nbh_generate_disc": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_float,

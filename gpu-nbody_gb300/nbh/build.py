@@ -19,7 +19,8 @@ OBJ_DIR = os.path.join(os.path.dirname(PKG), "_build")
 LIB = os.path.join(PKG, "libnbh.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["nbh_api.cu", "nbh_tree.cu", "nbh_force.cu", "nbh_theta.cu", "nbh_aux.cu", "nbh_host.cpp"]
+SOURCES = ["nbh_api.cu", "nbh_tree.cu", "nbh_force.cu", "nbh_theta.cu", "nbh_aux.cu", "nbh_diag.cu",
+           "nbh_host.cpp"]
 
 
 def nvcc() -> str:

@@ -34,7 +34,7 @@ def _f32(a):
 
 def make_config(theta=0.5, eps=0.05, dt=0.025, G=1.0, pool_factor=2.0, vote_width=None,
                 arith=L.NBH_ARITH_FMA, precise=False, stage_timing=False, use_graph=True,
-                device=0, theta2=0.0, eps2=0.0) -> L.NbhConfig:
+                device=0, theta2=0.0, eps2=0.0, force_threads=0, stack_cap=0, build_phases=0) -> L.NbhConfig:
     cfg = L.NbhConfig()
     L.load().nbh_config_default(C.byref(cfg))
     cfg.device = device
@@ -47,6 +47,7 @@ def make_config(theta=0.5, eps=0.05, dt=0.025, G=1.0, pool_factor=2.0, vote_widt
     cfg.precise = int(bool(precise))
     cfg.stage_timing = int(bool(stage_timing))
     cfg.use_graph = int(bool(use_graph))
+    cfg.force_threads, cfg.stack_cap, cfg.build_phases = force_threads, stack_cap, build_phases
     return cfg
 
 
@@ -154,6 +155,35 @@ class Simulation:
         out = [np.empty(idx.size, np.float64) for _ in range(3)]
         self._check(self._L.nbh_direct_f64(self._h, idx.size, idx.ctypes.data, *[o.ctypes.data for o in out]))
         return out
+
+    def diagnostics(self, potential: bool = False) -> list:
+        """Per-universe mass, centre of mass, momentum, angular momentum, kinetic and (with
+        potential=True, O(N^2)) potential energy, reduced on the GPU in FP64 (nbh_diagnostics)."""
+        nu = 1 if self.counts is None else len(self.counts)
+        arr = (L.NbhDiag * nu)()
+        got = self._L.nbh_diagnostics(self._h, L.NBH_DIAG_POTENTIAL if potential else 0, arr, nu)
+        if got < 0:
+            self._check(got)
+        out = []
+        for d in arr[:got]:
+            r = {"mass": d.mass, "com": list(d.com), "momentum": list(d.momentum),
+                 "angular_momentum": list(d.angular_momentum), "kinetic": d.kinetic, "max_depth": d.max_depth}
+            if d.has_potential:
+                r.update({"potential": d.potential, "potential_unsoftened": d.potential_unsoftened,
+                          "total": d.kinetic + d.potential})
+            out.append(r)
+        return out
+
+    def autotune(self) -> dict:
+        """Pick the force launch geometry and the build's insertion phases by timing them on
+        the loaded universes (nbh_autotune); later steps use the choice."""
+        t = L.NbhTune()
+        self._check(self._L.nbh_autotune(self._h, 0, C.byref(t)))
+        trials = [{"kind": ("force", "tree")[t.trial_kind[k]], "a": t.trial_a[k], "b": t.trial_b[k],
+                   "ms": t.trial_ms[k]} for k in range(t.trials)]
+        return {"force_threads": t.force_threads, "stack_cap": t.stack_cap, "build_phases": t.build_phases,
+                "max_depth": t.max_depth, "ms_force": t.ms_force, "ms_force_before": t.ms_force_before,
+                "ms_tree": t.ms_tree, "ms_tree_before": t.ms_tree_before, "trials": trials}
 
     def export_float4(self, dev_pos4: int | None, dev_vel4: int | None):
         self._check(self._L.nbh_export_float4(self._h, dev_pos4, dev_vel4))

@@ -83,7 +83,13 @@ typedef struct nbh_config {
                               extent / root centre of mass; 0: reference arithmetic */
     int32_t stage_timing;  /* 1: record per-stage CUDA-event times in nbh_stats */
     int32_t use_graph;     /* 1: replay each step as one captured CUDA graph (default) */
-    int32_t reserved[8];
+    int32_t force_threads; /* force launch geometry: threads per block, 64 / 128 / 256
+                              (0: 128); set by nbh_autotune */
+    int32_t stack_cap;     /* entries of each vote group's shared-memory stack, 64..256, a
+                              multiple of 8 (0: 256); trees deeper than (cap - 8) / 7 + 1
+                              levels take the per-level walk */
+    int32_t build_phases;  /* octree insertion launches: 1 (one pass) or 3 (0: 3) */
+    int32_t reserved[5];
 } nbh_config;
 
 /* Fills *cfg with the defaults: theta 0.5, eps 0.05, dt 0.025, G 1, pool 2.0,
@@ -200,6 +206,54 @@ int nbh_read_tree(nbh_sim* sim, int32_t* child, float* node4, int32_t* count,
  * This is the error yardstick of every force result (median / p99 relative error). */
 int nbh_direct_f64(nbh_sim* sim, int32_t nidx, const int32_t* idx,
                    double* ax, double* ay, double* az);
+
+/* Diagnostics of each universe (GPUBarnesHutNBodySimulation.java:305-365: printEnergy,
+ * printDepth, printImpulse), reduced on the GPU in FP64 from the current state, in a fixed
+ * order.  Energies and momenta use the state as stored: after a step, positions and
+ * velocities at the end of that step. */
+#define NBH_DIAG_POTENTIAL 1   /* also the O(N^2) pair potential (0.8 s at 1M bodies on GB300) */
+typedef struct nbh_diag {
+    double mass;                   /* sum m */
+    double com[3];                 /* sum m x / sum m */
+    double momentum[3];            /* sum m v (printImpulse, :347-365) */
+    double angular_momentum[3];    /* sum m x cross v, about the origin */
+    double kinetic;                /* sum m |v|^2 / 2 (:318-324) */
+    double potential;              /* -G sum_{i<j} m_i m_j / sqrt(r^2 + eps^2): the potential of
+                                      the softened force the step integrates */
+    double potential_unsoftened;   /* -G sum_{i<j} m_i m_j / r: the form of :326-335, where each
+                                      pair is added twice (`2 * e`, :334); here once */
+    int32_t max_depth;             /* printDepth (:341-345): the sim's tree depth, all universes */
+    int32_t has_potential;         /* 1 when the potentials were computed */
+} nbh_diag;
+/* Fills out[0 .. min(nout, universes)) and returns the number filled (>= 0) or an error. */
+int nbh_diagnostics(nbh_sim* sim, int32_t flags, nbh_diag* out, int32_t nout);
+
+/* Autotuner of the launch geometry (no counterpart in the reference, whose work-group sizes
+ * and stack depth are compile-time constants, calculateforce.cl:11-18 and the host's 16 x 16
+ * geometry).  On the loaded universes at their current positions it times every force
+ * geometry (threads per block 64 / 128 / 256 x stack capacities from the smallest the tree's
+ * depth allows, with 2 levels of headroom, to 256) as side-effect-free force launches that
+ * write a scratch buffer, and the tree stages with 1 and 3 insertion phases, then keeps the
+ * fastest of each for later steps.  Neither choice changes any result: the walk order, the
+ * arithmetic and the tree are the same for every geometry.  flags: 0.  Body state and the
+ * step counter are left as they were. */
+#define NBH_TUNE_MAX_TRIALS 16
+typedef struct nbh_tune {
+    int32_t force_threads;         /* chosen */
+    int32_t stack_cap;             /* chosen */
+    int32_t build_phases;          /* chosen */
+    int32_t max_depth;             /* tree depth the stack capacities were fitted to */
+    float   ms_force;              /* force launch of the choice */
+    float   ms_force_before;       /* force launch of the geometry in place before */
+    float   ms_tree;               /* tree stages of the choice */
+    float   ms_tree_before;        /* tree stages of the phases in place before */
+    int32_t trials;                /* entries used below */
+    int32_t trial_kind[NBH_TUNE_MAX_TRIALS];    /* 0 force, 1 tree */
+    int32_t trial_a[NBH_TUNE_MAX_TRIALS];       /* threads, or insertion phases */
+    int32_t trial_b[NBH_TUNE_MAX_TRIALS];       /* stack capacity (force) */
+    float   trial_ms[NBH_TUNE_MAX_TRIALS];      /* mean of 3 timed launches after 1 warm-up */
+} nbh_tune;
+int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out);
 
 /* ---- Learned per-body opening angle (no counterpart in the reference) ---------------- */
 

@@ -197,6 +197,54 @@ def direct_f64(x, y, z, m, eps, idx, G=1.0, eps2=None):
     return ax, ay, az
 
 
+def diagnostics_f64(x, y, z, vx, vy, vz, m, eps, G=1.0, potential=True, block=2048):
+    """FP64 restatement of nbh_diagnostics for one universe: mass, centre of mass, momentum
+    (printImpulse, GPUBarnesHutNBodySimulation.java:347-365), angular momentum, kinetic energy
+    (:318-324) and the pair potentials -G sum_{i<j} m_i m_j / sqrt(r^2 + eps^2) and
+    -G sum_{i<j} m_i m_j / r (each pair once; see reference_energy for :326-335)."""
+    x, y, z, vx, vy, vz, m = (np.asarray(a, dtype=np.float64) for a in (x, y, z, vx, vy, vz, m))
+    M = m.sum()
+    out = {"mass": M, "com": [float((m * x).sum() / M), float((m * y).sum() / M), float((m * z).sum() / M)],
+           "momentum": [float((m * vx).sum()), float((m * vy).sum()), float((m * vz).sum())],
+           "angular_momentum": [float((m * (y * vz - z * vy)).sum()), float((m * (z * vx - x * vz)).sum()),
+                                float((m * (x * vy - y * vx)).sum())],
+           "kinetic": float((0.5 * m * (vx * vx + vy * vy + vz * vz)).sum())}
+    if potential:
+        n = x.size
+        ps = pu = 0.0
+        e2 = float(np.float32(eps) * np.float32(eps))
+        for a in range(0, n, block):
+            b = min(n, a + block)
+            dx = x[a:b, None] - x[None, :]
+            dy = y[a:b, None] - y[None, :]
+            dz = z[a:b, None] - z[None, :]
+            r2 = dx * dx + dy * dy + dz * dz
+            mm = m[a:b, None] * m[None, :]
+            self_ = np.arange(a, b)[:, None] == np.arange(n)[None, :]
+            with np.errstate(divide="ignore"):
+                ps += np.where(self_, 0.0, mm / np.sqrt(r2 + e2)).sum()
+                pu += np.where(self_, 0.0, mm / np.sqrt(r2)).sum()
+        out["potential"] = -0.5 * G * ps
+        out["potential_unsoftened"] = -0.5 * G * pu
+    return out
+
+
+def reference_energy(x, y, z, vx, vy, vz, m):
+    """printEnergy (GPUBarnesHutNBodySimulation.java:305-339) as the reference computes it:
+    ekin = sum m v^2 / 2 with v = |v| (:318-324); epot = sum_{i<j} 2 m_i m_j / r, each pair
+    added twice (:326-335); etot = ekin - epot (:338).  Small N only (pairwise loop)."""
+    x, y, z, vx, vy, vz, m = (np.asarray(a, dtype=np.float64) for a in (x, y, z, vx, vy, vz, m))
+    ekin = epot = 0.0
+    n = x.size
+    for i in range(n):
+        v = np.sqrt(vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i])
+        ekin += m[i] * v * v / 2
+        for j in range(i + 1, n):
+            r = np.sqrt((x[i] - x[j]) ** 2 + (y[i] - y[j]) ** 2 + (z[i] - z[j]) ** 2)
+            epot += 2 * (m[i] * m[j]) / r
+    return {"ekin": ekin, "epot": epot, "etot": ekin - epot}
+
+
 def rel_force_error(ax, ay, az, rx, ry, rz):
     """|a - a_ref| / |a_ref| per body."""
     num = np.sqrt((ax - rx) ** 2 + (ay - ry) ** 2 + (az - rz) ** 2)

@@ -1,0 +1,70 @@
+"""Launch-geometry autotuner and the run-time force geometry on GB300: every geometry gives
+the same results, and the tuner leaves the simulation state as it found it."""
+import numpy as np
+import pytest
+
+from helpers import KEYS, acc_rel, gpu_sim, oracle_for, plummer
+
+pytestmark = pytest.mark.gpu
+
+
+def test_autotune_choice_changes_no_result():
+    n = 20000
+    arrs = plummer(n, seed=81)
+    a = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    b = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    a.load(*arrs)
+    b.load(*arrs)
+    a.step(2)
+    b.step(2)
+    before = b.stats()
+    t = b.autotune()
+    after = b.stats()
+    assert after["steps"] == before["steps"] and after["max_depth"] == before["max_depth"]
+    assert t["force_threads"] in (64, 128, 256) and 64 <= t["stack_cap"] <= 256 and t["build_phases"] in (1, 3)
+    assert t["max_depth"] == before["max_depth"]
+    assert (t["stack_cap"] - 8) // 7 + 1 >= t["max_depth"] or t["stack_cap"] == 256
+    assert any(tr["kind"] == "force" for tr in t["trials"]) and any(tr["kind"] == "tree" for tr in t["trials"])
+    assert t["ms_force"] <= t["ms_force_before"] + 1e-6 and t["ms_tree"] <= t["ms_tree_before"] + 1e-6
+    # state untouched by the tuning launches
+    sa, sb = a.read(), b.read()
+    for k in KEYS:
+        np.testing.assert_array_equal(sa[k], sb[k])
+    a.step(3)
+    b.step(3)
+    sa, sb = a.read(), b.read()
+    for k in KEYS:
+        np.testing.assert_array_equal(sa[k], sb[k])
+    assert a.stats()["interactions"] == b.stats()["interactions"]
+
+
+@pytest.mark.parametrize("vote,threads,cap", [(64, 64, 64), (64, 256, 96), (32, 64, 128), (16, 256, 64)])
+def test_force_geometries_match_oracle(vote, threads, cap):
+    """Block sizes and stack capacities, including a 64-entry stack that sends a 14-level
+    tree through the per-level walk (fast path only up to 9 levels)."""
+    n = 20000
+    arrs = plummer(n, seed=82)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=vote, force_threads=threads, stack_cap=cap)
+    g.load(*arrs)
+    o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=vote, fma=True)
+    o.load(*arrs)
+    g.step(2)
+    o.step(2)
+    assert g.stats()["interactions"] == o.interactions
+    rel, _ = acc_rel(g.read(), o.state())
+    assert rel.max() <= 1e-4, rel.max()
+
+
+def test_single_pass_build_gives_the_same_tree():
+    n = 30000
+    arrs = plummer(n, seed=83)
+    a = gpu_sim(theta=0.5, eps=0.05, dt=0.01, build_phases=1)
+    b = gpu_sim(theta=0.5, eps=0.05, dt=0.01, build_phases=3)
+    a.load(*arrs)
+    b.load(*arrs)
+    a.step(2)
+    b.step(2)
+    np.testing.assert_array_equal(a.tree()["sorted"], b.tree()["sorted"])
+    sa, sb = a.read(), b.read()
+    for k in KEYS:
+        np.testing.assert_array_equal(sa[k], sb[k])
