@@ -37,9 +37,9 @@ for _p in (os.path.join(ROOT, "gpu-nbody_gb300"), os.path.join(ROOT, "oracle")):
 
 METRIC = "ms/step at 1M bodies, plain vs learned-theta at equal p99 force error; Gint/s"
 DEFAULT_VOTE = 64                   # libnbh's default vote width (nbh_config_default)
-# Kernels in one fixed-angle step graph: bbox, build (3 insertion phases), link,
-# summarize, sort, force, integrate.
-GRAPH_LAUNCHES = 9
+# Kernels in one fixed-angle step graph at the default geometry: bbox, build (5 insertion
+# phases), link, summarize, sort, force, integrate.
+GRAPH_LAUNCHES = 11
 FLOPS_PER_INTERACTION = 20          # 3 sub, 3 fma (d^2+eps^2), rsqrt, 3 mul, 3 fma, ~7 more
 HBM_FALLBACK_GBS = 6800.0
 # DRAM bytes (read + write) of one force launch (vote width 64) on the 1,048,576-body
@@ -371,7 +371,7 @@ def main():
     # per-stage device times (eager launches with events between stages)
     hbm_peak, peak_src = _peaks()
     geometry = {} if tune is None else {"force_threads": tune["force_threads"], "stack_cap": tune["stack_cap"],
-                                        "build_phases": tune["build_phases"]}
+                                        "build_phases": tune["build_phases"], "build_buckets": tune["build_buckets"]}
     ts = new_sim(stage_timing=True, **geometry)
     ts.step(2)
     tstream = torch.cuda.ExternalStream(ts.stream, device=dev)
@@ -494,7 +494,7 @@ def main():
             "stages": stages,
             "roofline": roofline,
             "autotune": None if tune is None else {k: tune[k] for k in (
-                "force_threads", "stack_cap", "build_phases", "max_depth", "ms_force", "ms_force_before",
+                "force_threads", "stack_cap", "build_phases", "build_buckets", "max_depth", "ms_force", "ms_force_before",
                 "ms_tree", "ms_tree_before")},
             "e2e": {"value": e2e_ms / world, "unit": "ms/step", "h2d_bytes_per_step": 36 * n,
                     "d2h_bytes_per_step": 36 * n, "wall_ms_per_step": wall_ms,

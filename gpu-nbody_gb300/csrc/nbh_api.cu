@@ -49,7 +49,10 @@ struct nbh_sim {
     int theta_group = 0;           // 1: each vote group walks with its smallest angle
     int force_threads = 128;       // force launch geometry (nbh_autotune)
     int stack_cap = 256;
-    int build_phases = 3;          // octree insertion launches
+    int build_phases = 5;          // octree insertion launches
+    bool build_buckets = true;     // lock phases insert a 1/16 sample, the rest is built per slot
+    int4* buckets = nullptr;       // bucketed build: nbody records
+    int* bwork = nullptr;          // bucketed build: 2 * nbody entries
     ThetaDev* model = nullptr;     // installed model (device)
     float* model_prm = nullptr;    // its FP32 parameters (device)
     float* probe_theta = nullptr;  // per-body theta of the last force probe (device)
@@ -109,7 +112,7 @@ int grow(nbh_sim* sim, T** ptr, size_t count, size_t* cap_unused = nullptr) {
 void free_buffers(nbh_sim* sim) {
     void* ptrs[] = {sim->probe_theta, sim->feat, sim->clevel, sim->probe, sim->loff, sim->kids4, sim->node4, sim->vel, sim->acc, sim->kpos, sim->kvel, sim->child, sim->count,
                     sim->start, sim->arrive, sim->parent, sim->sorted, sim->ubody, sim->ubox,
-                    sim->uradius, sim->chunks, sim->warps, sim->staging, sim->theta_body};
+                    sim->uradius, sim->chunks, sim->warps, sim->staging, sim->theta_body, sim->buckets, sim->bwork};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     sim->kids4 = sim->node4 = sim->vel = sim->acc = sim->kpos = sim->kvel = nullptr;
@@ -123,6 +126,8 @@ void free_buffers(nbh_sim* sim) {
     sim->warps = nullptr;
     sim->staging = nullptr;
     sim->theta_body = nullptr;
+    sim->buckets = nullptr;
+    sim->bwork = nullptr;
     sim->cap_body = sim->cap_nodes = sim->cap_univ = sim->cap_chunks = sim->cap_warps = 0;
 }
 
@@ -150,6 +155,8 @@ StepParams step_params(const nbh_sim* sim) {
     p.theta_body = sim->theta_active ? sim->theta_body : nullptr;
     p.theta_group = sim->theta_group;
     p.stack_cap = sim->stack_cap;
+    p.buckets = sim->buckets;
+    p.bwork = sim->bwork;
     p.st = sim->st;
     p.ubody = sim->ubody;
     p.ubox = sim->ubox;
@@ -180,7 +187,7 @@ void enqueue_step(nbh_sim* sim, bool timed) {
     if (timed) cudaEventRecord(sim->ev[0], s);
     launch_bbox(p, sim->grid_bbox, s);
     if (timed) cudaEventRecord(sim->ev[1], s);
-    launch_build(p, sim->build_phases, s);
+    launch_build(p, sim->build_phases, sim->build_buckets, sim->sms, s);
     launch_link(p, sim->grid_sum, s);
     if (timed) cudaEventRecord(sim->ev[2], s);
     launch_summarize(p, ref, sim->grid_sum, s);
@@ -208,7 +215,7 @@ void enqueue_tree(nbh_sim* sim, const StepParams& p) {
     const bool ref = sim->cfg.arith == NBH_ARITH_REFERENCE;
     cudaStream_t s = sim->stream;
     launch_bbox(p, sim->grid_bbox, s);
-    launch_build(p, sim->build_phases, s);
+    launch_build(p, sim->build_phases, sim->build_buckets, sim->sms, s);
     launch_link(p, sim->grid_sum, s);
     launch_summarize(p, ref, sim->grid_sum, s);
     launch_sort(p, sim->grid_sort, s);
@@ -287,6 +294,8 @@ int alloc_for(nbh_sim* sim, int nbody, int nuniv, int nnodes, int nchunks, int n
     if ((e = grow(sim, &sim->loff, (size_t)ncells))) return e;
     if ((e = grow(sim, &sim->clevel, (size_t)ncells))) return e;
     if ((e = grow(sim, &sim->probe, (size_t)nbody))) return e;
+    if ((e = grow(sim, &sim->buckets, (size_t)nbody))) return e;
+    if ((e = grow(sim, &sim->bwork, 2 * (size_t)nbody))) return e;
     if ((e = grow(sim, &sim->probe_theta, (size_t)nbody))) return e;
     if ((e = grow(sim, &sim->feat, (size_t)nbody * kMlpIn))) return e;
     if ((e = grow(sim, &sim->start, (size_t)ncells))) return e;
@@ -462,8 +471,10 @@ int nbh_create(const nbh_config* cfg_in, nbh_sim** out) {
     if (!force_geometry_valid(cfg.vote_width, threads, cap))
         return fail(nullptr, NBH_ERR_INVALID, "force_threads must be 64, 128 or 256 and stack_cap a multiple of 8 "
                                               "in [64, 256]");
-    if (cfg.build_phases != 0 && cfg.build_phases != 1 && cfg.build_phases != 3)
-        return fail(nullptr, NBH_ERR_INVALID, "build_phases must be 1 or 3");
+    if (cfg.build_phases != 0 && cfg.build_phases != 1 && cfg.build_phases != 3 && cfg.build_phases != 5)
+        return fail(nullptr, NBH_ERR_INVALID, "build_phases must be 1, 3 or 5");
+    if (cfg.build_buckets < 0 || cfg.build_buckets > 2)
+        return fail(nullptr, NBH_ERR_INVALID, "build_buckets must be 0 (default), 1 (on) or 2 (off)");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0) return fail(nullptr, NBH_ERR_NODEVICE, "no CUDA device");
@@ -479,7 +490,8 @@ int nbh_create(const nbh_config* cfg_in, nbh_sim** out) {
     sim->device = cfg.device;
     sim->force_threads = threads;
     sim->stack_cap = cap;
-    sim->build_phases = cfg.build_phases ? cfg.build_phases : 3;
+    sim->build_phases = cfg.build_phases ? cfg.build_phases : 5;
+    sim->build_buckets = cfg.build_buckets != 2;
     sim->sms = prop.multiProcessorCount;
     if ((e = cudaSetDevice(cfg.device)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&sim->stream, cudaStreamNonBlocking)) != cudaSuccess ||
@@ -999,29 +1011,35 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
             best_c = g.second;
         }
     }
-    // tree stages with one and three insertion phases
+    // tree stages: one lock pass; three or five lock phases; three or five with the bucketed
+    // completion
     const int phases_before = sim->build_phases;
+    const bool buckets_before = sim->build_buckets;
     float best_tree = 1e30f;
     int best_ph = phases_before;
-    const int phase_c[2] = {1, 3};
-    for (int ph : phase_c) {
+    bool best_bk = buckets_before;
+    const int tree_c[5][2] = {{1, 0}, {3, 0}, {5, 0}, {3, 1}, {5, 1}};
+    for (const auto& tc : tree_c) {
         if (err != cudaSuccess) break;
-        sim->build_phases = ph;
+        sim->build_phases = tc[0];
+        sim->build_buckets = tc[1] != 0;
         StepParams p = step_params(sim);
         p.theta_body = nullptr;
         float ms = 0.0f;
         err = timed([&] { enqueue_tree(sim, p); }, &ms);
         if (err != cudaSuccess) break;
-        add_trial(1, ph, 0, ms);
-        if (ph == phases_before) out->ms_tree_before = ms;
+        add_trial(1, tc[0], tc[1], ms);
+        if (tc[0] == phases_before && (tc[1] != 0) == (buckets_before && phases_before != 1)) out->ms_tree_before = ms;
         if (ms < best_tree) {
             best_tree = ms;
-            best_ph = ph;
+            best_ph = tc[0];
+            best_bk = tc[1] != 0;
         }
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     sim->build_phases = phases_before;
+    sim->build_buckets = buckets_before;
     if (err != cudaSuccess) return cuda_fail(sim, "nbh_autotune", err);
     CK(cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -1033,11 +1051,13 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
     sim->force_threads = best_t;
     sim->stack_cap = best_c;
     sim->build_phases = best_ph;
+    sim->build_buckets = best_bk;
     if ((e = set_geometry(sim))) return e;
     drop_graph(sim);
     out->force_threads = best_t;
     out->stack_cap = best_c;
     out->build_phases = best_ph;
+    out->build_buckets = best_bk ? 1 : 2;
     out->ms_force = best_ms;
     out->ms_tree = best_tree;
     return NBH_OK;

@@ -55,7 +55,11 @@ struct DevState {
     int theta_since;     // learned theta: steps up to this index use the fixed theta
     int theta_every;     // learned theta: steps between evaluations of the model (>= 1)
     unsigned long long interactions;   // accepted force evaluations of the last step
-    unsigned long long pad2[3];
+    int bucket_fill;     // bucketed build: entries handed out in the bucket work list
+    int nbuckets;        // bucketed build: non-empty slots of the sampled tree
+    int bucket_next;     // bucketed build: work counter of the subtree builders
+    int pad1;
+    unsigned long long pad2;
     // Build contention meters, spread over kDiagSlots addresses so that counting does not
     // itself serialise: descents that found their slot locked, and lost lock races.
     int lock_waits[32];
@@ -99,6 +103,8 @@ struct StepParams {
     float dt;
     float G;
     int precise;
+    int4* buckets;       // bucketed build: (slot, first entry, bodies, 0) per non-empty slot
+    int* bwork;          // bucketed build: 2 * nbody entries (bodies of each bucket, ping-pong)
     int stack_cap;       // entries of each force group's shared-memory stack
     int theta_group;     // per-body theta: 1 = each vote group walks with its smallest angle
     int feat_gate;       // force launch gated on the learned-theta schedule: 0 none,

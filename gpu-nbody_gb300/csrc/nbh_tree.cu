@@ -101,6 +101,9 @@ __global__ void __launch_bounds__(256) bbox_kernel(StepParams p) {
         p.count[k] = 0;
         p.start[k] = p.ubody[u];
         p.uradius[u] = radius;
+        int4* bc = reinterpret_cast<int4*>(p.kids4 + ((size_t)k << 3));   // bucket counters
+        bc[0] = make_int4(0, 0, 0, 0);
+        bc[1] = make_int4(0, 0, 0, 0);
         // fresh extents for the next step
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
@@ -114,6 +117,9 @@ __global__ void __launch_bounds__(256) bbox_kernel(StepParams p) {
         st->bbox_ticket = 0;
         st->step += 1;
         st->force_next = 0;
+        st->bucket_fill = 0;
+        st->nbuckets = 0;
+        st->bucket_next = 0;
         for (int j = 0; j < kDiagSlots; ++j) st->lock_waits[j] = st->cas_misses[j] = 0;
         st->interactions = 0ull;
     }
@@ -129,25 +135,33 @@ __global__ void __launch_bounds__(256) bbox_kernel(StepParams p) {
 // the lock.  Failed locks retry from the same node (the tree only grows) with a bounded,
 // backed-off wait.
 //
-// Insertion runs in three phases (three launches): first one body of every 256-body
-// chunk, then one in 16, then the rest.  The octree of a set of bodies does not depend
-// on the order the bodies arrive in, so the phases build exactly the tree a single pass
-// would; what they change is contention.  In one pass every body of a universe that is
-// resident at once descends into the same empty top levels and waits on each split there
-// in turn (in a batch of small universes that is every body).  After the first two
-// phases the top of each tree already holds about 1/16 of its bodies, so the last phase's
-// descents spread over many cells and rarely meet a locked slot.
-constexpr int kBuildPhases = 3;
-__host__ __device__ constexpr int phase_bodies(int phase) {   // per full 256-body chunk
-    return phase < 0 ? 256 : (phase == 0 ? 1 : (phase == 1 ? 15 : 240));
+// Insertion runs in phases (one launch each): first one body of every 256-body chunk,
+// then more and more of each chunk (3 phases: 1 in 16, then the rest; 5 phases: 1 in 64,
+// 1 in 16, 1 in 4, then the rest).  The octree of a set of bodies does not depend on the
+// order the bodies arrive in, so the phases build exactly the tree a single pass would;
+// what they change is contention.  In one pass every body of a universe that is resident
+// at once descends into the same empty top levels and waits on each split there in turn
+// (in a batch of small universes that is every body).  After the early phases the top of
+// each tree already holds a sample of its bodies, so later descents spread over many cells
+// and rarely meet a locked slot.
+//
+// A phase takes, in each chunk, the offsets that are multiples of `stride` but (ratio > 0)
+// not multiples of stride * ratio, i.e. the ones an earlier phase did not take.
+struct BuildPhase {
+    int stride, ratio;
+};
+__host__ __device__ constexpr int phase_bodies(BuildPhase ph) {   // per full 256-body chunk
+    return ph.ratio > 0 ? 256 / ph.stride - 256 / (ph.stride * ph.ratio) : 256 / ph.stride;
 }
-// Offset inside its chunk of the phase's idx-th body: 0; 16, 32, ..., 240; the rest.
-// Phase -1 is a single pass over every body.
-__device__ __forceinline__ int phase_offset(int phase, int idx) {
-    return phase < 0 ? idx : (phase == 0 ? 0 : (phase == 1 ? 16 * (idx + 1) : idx + idx / 15 + 1));
+// Offset inside its chunk of the phase's idx-th body.
+__device__ __forceinline__ int phase_offset(BuildPhase ph, int idx) {
+    return ph.ratio > 0 ? ph.stride * (idx + idx / (ph.ratio - 1) + 1) : ph.stride * idx;
 }
+constexpr BuildPhase kOnePass[1] = {{1, 0}};
+constexpr BuildPhase kThreePhases[3] = {{256, 0}, {16, 16}, {1, 16}};
+constexpr BuildPhase kFivePhases[5] = {{256, 0}, {64, 4}, {16, 4}, {4, 4}, {1, 4}};
 
-__global__ void __launch_bounds__(256) build_kernel(StepParams p, int phase) {
+__global__ void __launch_bounds__(256) build_kernel(StepParams p, BuildPhase phase, bool zero_counts) {
     if (load_status(p.st)) return;
     int local_max = 1;
     int waits = 0, misses = 0;
@@ -233,6 +247,11 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p, int phase) {
                             reinterpret_cast<int4*>(cc)[1] = make_int4(kNull, kNull, kNull, kNull);
                             p.arrive[cell - nbody] = 0;
                             p.clevel[cell - nbody] = depth - 1;   // root = level 0
+                            if (zero_counts) {   // bucket counters of the sampled tree
+                                int4* bc = reinterpret_cast<int4*>(p.kids4 + ((size_t)(cell - nbody) << 3));
+                                bc[0] = make_int4(0, 0, 0, 0);
+                                bc[1] = make_int4(0, 0, 0, 0);
+                            }
                             if (patch < 0) patch = cell;
                             else cell_child(p, cur)[cpath] = cell;
                             const int opath = octant(cx, cy, cz, op.x, op.y, op.z);
@@ -265,6 +284,418 @@ finish:
     if (local_max > ld_relaxed(&p.st->max_depth)) atomicMax(&p.st->max_depth, local_max);
     if (waits) atomicAdd(&p.st->lock_waits[blockIdx.x % kDiagSlots], waits);
     if (misses) atomicAdd(&p.st->cas_misses[blockIdx.x % kDiagSlots], misses);
+}
+
+// -------------------------------------------------------------------------------------
+// Bucketed completion of the build.  After the lock phases have inserted a 1/16 sample
+// of every chunk (the "sampled tree"), each remaining body finds, by a read-only descent,
+// the slot of the sampled tree it would be inserted into.  The bodies headed for one slot
+// (its bucket, plus the body already in it) are exactly those of the subtree that replaces
+// the slot in the final tree, and no other body touches that subtree, so one warp builds
+// it alone: no locks, no release fences (later kernels read it across the kernel
+// boundary).  The tree is the one the lock insertion builds (it is order independent):
+// a cell exists for every octant prefix shared by two or more bodies, with the same
+// centres (the same arithmetic from the same parent centre and half-width).
+//
+// Bucket counters of a sampled-tree cell live in its kids4 block, which summarize
+// overwrites later in the step: ints 0..7 = bodies headed for slot j, 8..15 = first entry
+// of slot j's bucket in the work list, 16..19 = the cell's centre and half-width.
+__device__ __forceinline__ int* bucket_counters(const StepParams& p, int c) {
+    return reinterpret_cast<int*>(p.kids4 + ((size_t)(c - p.nbody) << 3));
+}
+constexpr BuildPhase kBucketBodies = {1, 16};   // the bodies outside the 1/16 sample
+
+// (1) locate: read-only descent of each remaining body to its slot; the slot index goes
+// to parent[b] (scratch: the link pass writes the body's parent later).
+__global__ void __launch_bounds__(256) bucket_locate_kernel(StepParams p) {
+    if (load_status(p.st)) return;
+    const int nbody = p.nbody;
+    const int per = phase_bodies(kBucketBodies);
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (long long)p.nchunks * per) return;
+    const int4 ck = p.chunks[g / per];
+    const int b = ck.y + phase_offset(kBucketBodies, (int)(g % per));
+    if (b >= ck.z) return;
+    const int root = p.nnodes - ck.x;
+    const float4 rc = p.node4[root];
+    const float4 bp = p.node4[b];
+    float r = p.uradius[ck.x];
+    float cx = rc.x, cy = rc.y, cz = rc.z;
+    int node = root, depth = 1;
+    int path = octant(cx, cy, cz, bp.x, bp.y, bp.z);
+    int ch = __ldg(cell_child(p, node) + path);
+    while (ch >= nbody) {
+        if (ch >= node || ++depth > kMaxDepth) {
+            raise_error(p.st, NBH_ERR_DEPTH);
+            return;
+        }
+        node = ch;
+        const float h = r * 0.5f;
+        cx = __fadd_rn(__fsub_rn(cx, h), (path & 1) ? r : 0.0f);
+        cy = __fadd_rn(__fsub_rn(cy, h), (path & 2) ? r : 0.0f);
+        cz = __fadd_rn(__fsub_rn(cz, h), (path & 4) ? r : 0.0f);
+        r = h;
+        path = octant(cx, cy, cz, bp.x, bp.y, bp.z);
+        ch = __ldg(cell_child(p, node) + path);
+    }
+    p.parent[b] = ((node - nbody) << 3) | path;
+    int* bc = bucket_counters(p, node);
+    if (atomicAdd(bc + path, 1) == 0) {
+        // the first body headed for a slot of `node` records the cell's centre and
+        // half-width for the subtree builder (every descent computes the same values)
+        reinterpret_cast<float4*>(bc)[4] = make_float4(cx, cy, cz, r);
+    }
+}
+
+// (2) allocate: per sampled-tree cell, the work-list entries of its non-empty slots
+// (bodies headed there, plus the body the slot holds) and one bucket record each.
+__global__ void __launch_bounds__(256) bucket_alloc_kernel(StepParams p) {
+    if (load_status(p.st)) return;
+    const int nbody = p.nbody;
+    const int c = ld_relaxed(&p.st->bottom) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const bool valid = c <= p.nnodes;
+    int cnt[8], held[8];
+    int total = 0, nb = 0;
+    if (valid) {
+        const int4* bc = reinterpret_cast<const int4*>(bucket_counters(p, c));
+        const int4 a0 = bc[0], a1 = bc[1];
+        const int4* ch = reinterpret_cast<const int4*>(cell_child(p, c));
+        const int4 s0 = ch[0], s1 = ch[1];
+        const int cc[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const int ss[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            cnt[j] = cc[j];
+            held[j] = (cc[j] > 0 && ss[j] >= 0 && ss[j] < nbody) ? ss[j] : kNull;
+            total += cc[j] > 0 ? cc[j] + (held[j] >= 0 ? 1 : 0) : 0;
+            nb += cc[j] > 0 ? 1 : 0;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) cnt[j] = 0, held[j] = kNull;
+    }
+    // warp-aggregated allocation of entries and bucket records
+    const int lane = threadIdx.x & 31;
+    int te = total, tb = nb;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int ue = __shfl_up_sync(0xffffffffu, te, o), ub = __shfl_up_sync(0xffffffffu, tb, o);
+        if (lane >= o) te += ue, tb += ub;
+    }
+    int be = 0, bb = 0;
+    if (lane == 31) {
+        be = atomicAdd(&p.st->bucket_fill, te);
+        bb = atomicAdd(&p.st->nbuckets, tb);
+    }
+    be = __shfl_sync(0xffffffffu, be, 31) + te - total;
+    bb = __shfl_sync(0xffffffffu, bb, 31) + tb - nb;
+    if (!valid || total == 0) return;
+    int* bcw = bucket_counters(p, c);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (cnt[j] <= 0) continue;
+        bcw[8 + j] = be;
+        p.buckets[bb++] = make_int4(((c - nbody) << 3) | j, be, cnt[j], held[j]);
+        be += cnt[j] + (held[j] >= 0 ? 1 : 0);
+    }
+}
+
+// (3) scatter: each remaining body takes an entry of its slot's bucket.
+__global__ void __launch_bounds__(256) bucket_scatter_kernel(StepParams p) {
+    if (load_status(p.st)) return;
+    const int per = phase_bodies(kBucketBodies);
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (long long)p.nchunks * per) return;
+    const int4 ck = p.chunks[g / per];
+    const int b = ck.y + phase_offset(kBucketBodies, (int)(g % per));
+    if (b >= ck.z) return;
+    const int slot = p.parent[b];
+    int* bc = bucket_counters(p, p.nbody + (slot >> 3));
+    const int j = slot & 7;
+    p.bwork[bc[8 + j] + atomicSub(bc + j, 1) - 1] = b;
+}
+
+// (4) build: one warp per bucket builds the bucket's subtree by splitting its bodies by
+// octant, level by level (depth first over a shared-memory task stack), writing each new
+// cell's 8 slots once with their final values, then stores the subtree's root into the
+// slot.  Subtrees of at most 32 bodies are built in registers (one body per lane, octant
+// splits by ballots over lane masks): a counting pass sizes the subtree so one atomic takes
+// all its cells, then the writing pass hands them out parents first.  Larger buckets split
+// through the two halves of bwork until a part has at most 32 bodies.
+struct BucketTask {
+    int cell, level, lo, hi, buf;
+    float cx, cy, cz, r;       // centre and half-width of `cell`
+};
+struct SmallTask {
+    unsigned mask;             // lanes holding the task's bodies
+    int cell, level;
+    float cx, cy, cz, r;
+};
+constexpr int kBucketWarps = 4;
+// Children are pushed largest first, so every stacked sibling holds at most half of its
+// parent's bodies: the stack stays within 7 log2(m) + 8 entries for a bucket of m bodies
+// (155 for m up to 2^21; 43 for the register subtrees of at most 32 bodies).
+constexpr int kBucketStack = 160;
+constexpr int kSmallStack = 48;
+
+// Stack position of each child cell among the nc cells pushed now: the largest deepest.
+__device__ __forceinline__ int deeper_rank(int mycnt, int lane) {
+    int deeper = 0;
+#pragma unroll
+    for (int o2 = 0; o2 < 8; ++o2) {
+        const int n2 = __shfl_sync(0xffffffffu, mycnt, o2);
+        deeper += (n2 >= 2 && (n2 > mycnt || (n2 == mycnt && o2 < lane))) ? 1 : 0;
+    }
+    return deeper;
+}
+
+// The subtree of the m <= 32 bodies src[lo, lo + m) below a cell of level `level` with the
+// given centre and half-width.  cell >= 0: that cell exists already (its slots are written
+// here); cell < 0: it is taken from the pool with the rest.  Returns the subtree's root cell
+// (or -1 after raising an error).  Whole-warp call.
+__device__ int build_small(const StepParams& p, const int* __restrict__ src, int lo, int m, int cell, int level,
+                           float cx, float cy, float cz, float r, SmallTask* st, int& local_max) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int nbody = p.nbody;
+    int b = 0;
+    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (lane < m) {
+        b = src[lo + lane];
+        q = p.node4[b];
+    }
+    const unsigned all = m >= 32 ? 0xffffffffu : ((1u << m) - 1u);
+    int base = 0, next = 0;
+    for (int pass = 0; pass < 2; ++pass) {           // 0: count the cells, 1: build
+        int made = 0;
+        if (pass == 1) {
+            if (lane == 0) base = atomicSub(&p.st->bottom, next);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base - next <= nbody) {
+                raise_error(p.st, NBH_ERR_POOL);
+                return -1;
+            }
+            made = 0;
+        }
+        int root = cell;
+        if (cell < 0) root = pass == 1 ? base - 1 - made++ : (made++, 0);
+        if (lane == 0) st[0] = SmallTask{all, root, level, cx, cy, cz, r};
+        int top = 1;
+        __syncwarp();
+        while (top > 0) {
+            const SmallTask t = st[--top];
+            __syncwarp();
+            const bool member = (t.mask >> lane) & 1u;
+            const int o = member ? octant(t.cx, t.cy, t.cz, q.x, q.y, q.z) : -1;
+            unsigned mybal = 0;
+#pragma unroll
+            for (int oc = 0; oc < 8; ++oc) {
+                const unsigned bal = __ballot_sync(0xffffffffu, o == oc);
+                if (lane == oc) mybal = bal;
+            }
+            const int mycnt = __popc(mybal);
+            const bool is_cell = lane < 8 && mycnt >= 2;
+            const unsigned balc = __ballot_sync(0xffffffffu, is_cell);
+            const int nc = __popc(balc);
+            if (nc > 0 && (t.level + 2 > kMaxDepth || top + nc > kSmallStack)) {   // coincident bodies
+                raise_error(p.st, NBH_ERR_DEPTH);
+                return -1;
+            }
+            const int deeper = deeper_rank(mycnt, lane);
+            const int single = __shfl_sync(0xffffffffu, b, lane < 8 && mycnt == 1 ? __ffs(mybal) - 1 : 0);
+            if (lane < 8) {
+                int v = kNull;
+                if (mycnt == 1) {
+                    v = single;
+                    local_max = max(local_max, t.level + 1);
+                } else if (mycnt >= 2) {
+                    v = pass == 1 ? base - 1 - made - __popc(balc & lt) : 0;
+                    const float h = t.r * 0.5f;
+                    st[top + deeper] = SmallTask{mybal, v, t.level + 1,
+                                                 __fadd_rn(__fsub_rn(t.cx, h), (lane & 1) ? t.r : 0.0f),
+                                                 __fadd_rn(__fsub_rn(t.cy, h), (lane & 2) ? t.r : 0.0f),
+                                                 __fadd_rn(__fsub_rn(t.cz, h), (lane & 4) ? t.r : 0.0f), h};
+                }
+                if (pass == 1) cell_child(p, t.cell)[lane] = v;
+            }
+            if (pass == 1 && lane == 0) {
+                p.arrive[t.cell - nbody] = 0;
+                p.clevel[t.cell - nbody] = t.level;
+            }
+            made += nc;
+            top += nc;
+            __syncwarp();
+        }
+        if (pass == 0) next = made;
+        else return root;
+    }
+    return -1;
+}
+
+__global__ void __launch_bounds__(32 * kBucketWarps) bucket_build_kernel(StepParams p) {
+    __shared__ BucketTask stack_all[kBucketWarps][kBucketStack];
+    __shared__ SmallTask small_all[kBucketWarps][kSmallStack];
+    if (load_status(p.st)) return;
+    BucketTask* stack = stack_all[threadIdx.x >> 5];
+    SmallTask* sstack = small_all[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int nbody = p.nbody;
+    const int nb = ld_relaxed(&p.st->nbuckets);
+    int local_max = 1;
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(&p.st->bucket_next, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= nb) break;
+        const int4 bk = p.buckets[item];
+        const int c = nbody + (bk.x >> 3), j = bk.x & 7;
+        const int start = bk.y, k = bk.z;
+        const int m = k + (bk.w >= 0 ? 1 : 0);
+        if (bk.w >= 0 && lane == 0) p.bwork[start + k] = bk.w;
+        __syncwarp();
+        // cell c's centre and half-width, recorded by the locate pass
+        const float4 g = reinterpret_cast<const float4*>(bucket_counters(p, c))[4];
+        const int clev = p.clevel[c - nbody];
+        int* slot = cell_child(p, c) + j;
+        if (m == 1) {                                 // a single body: the slot takes it
+            if (lane == 0) *slot = p.bwork[start];
+            local_max = max(local_max, clev + 1);
+            continue;
+        }
+        if (clev + 2 > kMaxDepth) {
+            raise_error(p.st, NBH_ERR_DEPTH);
+            return;
+        }
+        // the subtree's root: the child of c in octant j
+        const float h0 = g.w * 0.5f;
+        const float rcx = __fadd_rn(__fsub_rn(g.x, h0), (j & 1) ? g.w : 0.0f);
+        const float rcy = __fadd_rn(__fsub_rn(g.y, h0), (j & 2) ? g.w : 0.0f);
+        const float rcz = __fadd_rn(__fsub_rn(g.z, h0), (j & 4) ? g.w : 0.0f);
+        int root;
+        if (m <= 32) {
+            root = build_small(p, p.bwork, start, m, -1, clev + 1, rcx, rcy, rcz, h0, sstack, local_max);
+            if (root < 0) return;
+            if (lane == 0) *slot = root;
+            continue;
+        }
+        if (lane == 0) root = atomicSub(&p.st->bottom, 1) - 1;
+        root = __shfl_sync(0xffffffffu, root, 0);
+        if (root <= nbody) {
+            raise_error(p.st, NBH_ERR_POOL);
+            return;
+        }
+        if (lane == 0) stack[0] = BucketTask{root, clev + 1, start, start + m, 0, rcx, rcy, rcz, h0};
+        int top = 1;
+        __syncwarp();
+        bool ok = true;
+        while (top > 0) {
+            const BucketTask t = stack[--top];
+            __syncwarp();
+            const int* src = p.bwork + (t.buf ? nbody : 0);
+            int* dst = p.bwork + (t.buf ? 0 : nbody);
+            if (t.hi - t.lo <= 32) {                  // small enough for the register builder
+                if (build_small(p, src, t.lo, t.hi - t.lo, t.cell, t.level, t.cx, t.cy, t.cz, t.r, sstack,
+                                local_max) < 0) {
+                    ok = false;
+                    break;
+                }
+                continue;
+            }
+            // pass 1: bodies per octant (lane o < 8 holds octant o's count)
+            int mycnt = 0;
+            for (int base = t.lo; base < t.hi; base += 32) {
+                const int i = base + lane;
+                int o = -1;
+                if (i < t.hi) {
+                    const float4 q = p.node4[src[i]];
+                    o = octant(t.cx, t.cy, t.cz, q.x, q.y, q.z);
+                }
+#pragma unroll
+                for (int oc = 0; oc < 8; ++oc) {
+                    const int n = __popc(__ballot_sync(0xffffffffu, o == oc));
+                    if (lane == oc) mycnt += n;
+                }
+            }
+            // exclusive offsets of the octants (lanes 0..7)
+            int myoff = mycnt;
+#pragma unroll
+            for (int o2 = 1; o2 < 8; o2 <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, myoff, o2);
+                if (lane >= o2) myoff += v;
+            }
+            myoff -= mycnt;
+            // pass 2: bodies to dst in octant order
+            int run = 0;                              // lane o: bodies of octant o placed so far
+            for (int base = t.lo; base < t.hi; base += 32) {
+                const int i = base + lane;
+                int o = -1, b = 0;
+                if (i < t.hi) {
+                    b = src[i];
+                    const float4 q = p.node4[b];
+                    o = octant(t.cx, t.cy, t.cz, q.x, q.y, q.z);
+                }
+                unsigned mine = 0;
+#pragma unroll
+                for (int oc = 0; oc < 8; ++oc) {
+                    const unsigned bal = __ballot_sync(0xffffffffu, o == oc);
+                    if (o == oc) mine = bal;
+                    if (lane == oc) run += __popc(bal);
+                }
+                const int slot_base = __shfl_sync(0xffffffffu, myoff + run, o < 0 ? 0 : o);
+                // slot_base counts this chunk's bodies of octant o already: subtract them
+                if (o >= 0) dst[t.lo + slot_base - __popc(mine) + __popc(mine & lt)] = b;
+            }
+            __syncwarp();
+            // children: empty, one body, or a cell (allocated together)
+            const bool is_cell = lane < 8 && mycnt >= 2;
+            const unsigned balc = __ballot_sync(0xffffffffu, is_cell);
+            const int nc = __popc(balc);
+            int cbase = 0;
+            if (nc > 0) {
+                if (t.level + 2 > kMaxDepth || top + nc > kBucketStack) {   // coincident bodies
+                    raise_error(p.st, NBH_ERR_DEPTH);
+                    ok = false;
+                    break;
+                }
+                if (lane == 0) cbase = atomicSub(&p.st->bottom, nc);
+                cbase = __shfl_sync(0xffffffffu, cbase, 0);
+                if (cbase - nc <= nbody) {
+                    raise_error(p.st, NBH_ERR_POOL);
+                    ok = false;
+                    break;
+                }
+            }
+            const int deeper = deeper_rank(mycnt, lane);
+            if (lane < 8) {
+                int v = kNull;
+                if (mycnt == 1) {
+                    v = dst[t.lo + myoff];
+                    local_max = max(local_max, t.level + 1);
+                } else if (mycnt >= 2) {
+                    v = cbase - 1 - __popc(balc & lt);
+                    const float h = t.r * 0.5f;
+                    stack[top + deeper] = BucketTask{v, t.level + 1, t.lo + myoff, t.lo + myoff + mycnt, t.buf ^ 1,
+                                                     __fadd_rn(__fsub_rn(t.cx, h), (lane & 1) ? t.r : 0.0f),
+                                                     __fadd_rn(__fsub_rn(t.cy, h), (lane & 2) ? t.r : 0.0f),
+                                                     __fadd_rn(__fsub_rn(t.cz, h), (lane & 4) ? t.r : 0.0f), h};
+                }
+                cell_child(p, t.cell)[lane] = v;
+            }
+            if (lane == 0) {
+                p.arrive[t.cell - nbody] = 0;
+                p.clevel[t.cell - nbody] = t.level;
+            }
+            top += nc;
+            __syncwarp();
+        }
+        if (!ok) return;
+        if (lane == 0) *slot = root;
+    }
+    // :199; the maximum persists across steps, so the atomic is rarely needed
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) local_max = max(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
+    if (lane == 0 && local_max > ld_relaxed(&p.st->max_depth)) atomicMax(&p.st->max_depth, local_max);
 }
 
 // -------------------------------------------------------------------------------------
@@ -442,16 +873,24 @@ void launch_bbox(const StepParams& p, int grid, cudaStream_t s) {
     if (p.precise) bbox_kernel<true><<<grid, 256, 0, s>>>(p);
     else bbox_kernel<false><<<grid, 256, 0, s>>>(p);
 }
-void launch_build(const StepParams& p, int phases, cudaStream_t s) {
-    if (phases == 1) {      // a single pass over every body (phase index -1)
-        const long long bodies = (long long)p.nchunks * 256;
-        build_kernel<<<(unsigned)((bodies + 255) / 256), 256, 0, s>>>(p, -1);
-        return;
+void launch_build(const StepParams& p, int phases, bool buckets, int sms, cudaStream_t s) {
+    const BuildPhase* sched = phases == 1 ? kOnePass : (phases == 5 ? kFivePhases : kThreePhases);
+    int count = phases == 1 ? 1 : (phases == 5 ? 5 : 3);
+    buckets = buckets && phases != 1;
+    if (buckets) count -= phases == 5 ? 2 : 1;   // the lock phases insert the 1/16 sample only
+    for (int k = 0; k < count; ++k) {
+        const long long bodies = (long long)p.nchunks * phase_bodies(sched[k]);
+        build_kernel<<<(unsigned)((bodies + 255) / 256), 256, 0, s>>>(p, sched[k], buckets);
     }
-    for (int phase = 0; phase < kBuildPhases; ++phase) {
-        const long long bodies = (long long)p.nchunks * phase_bodies(phase);
-        build_kernel<<<(unsigned)((bodies + 255) / 256), 256, 0, s>>>(p, phase);
-    }
+    if (!buckets) return;
+    const long long rest = (long long)p.nchunks * phase_bodies(kBucketBodies);
+    const unsigned grid_rest = (unsigned)((rest + 255) / 256);
+    bucket_locate_kernel<<<grid_rest, 256, 0, s>>>(p);
+    // every cell of the sampled tree: at most one per sampled body plus the roots
+    const long long cells = (long long)p.nchunks * 16 + p.nuniv;
+    bucket_alloc_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(p);
+    bucket_scatter_kernel<<<grid_rest, 256, 0, s>>>(p);
+    bucket_build_kernel<<<8 * sms, 32 * kBucketWarps, 0, s>>>(p);
 }
 void launch_link(const StepParams& p, int grid, cudaStream_t s) {
     link_kernel<<<grid, 256, 0, s>>>(p);

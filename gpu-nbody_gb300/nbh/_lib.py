@@ -44,7 +44,8 @@ class NbhConfig(C.Structure):
         ("dt", C.c_float), ("G", C.c_float), ("pool_factor", C.c_float),
         ("vote_width", C.c_int32), ("arith", C.c_int32), ("precise", C.c_int32),
         ("stage_timing", C.c_int32), ("use_graph", C.c_int32), ("force_threads", C.c_int32),
-        ("stack_cap", C.c_int32), ("build_phases", C.c_int32), ("reserved", C.c_int32 * 5),
+        ("stack_cap", C.c_int32), ("build_phases", C.c_int32), ("build_buckets", C.c_int32),
+        ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -75,7 +76,7 @@ NBH_TUNE_MAX_TRIALS = 16
 class NbhTune(C.Structure):
     _fields_ = [
         ("force_threads", C.c_int32), ("stack_cap", C.c_int32), ("build_phases", C.c_int32),
-        ("max_depth", C.c_int32), ("ms_force", C.c_float), ("ms_force_before", C.c_float),
+        ("build_buckets", C.c_int32), ("max_depth", C.c_int32), ("ms_force", C.c_float), ("ms_force_before", C.c_float),
         ("ms_tree", C.c_float), ("ms_tree_before", C.c_float), ("trials", C.c_int32),
         ("trial_kind", C.c_int32 * NBH_TUNE_MAX_TRIALS), ("trial_a", C.c_int32 * NBH_TUNE_MAX_TRIALS),
         ("trial_b", C.c_int32 * NBH_TUNE_MAX_TRIALS), ("trial_ms", C.c_float * NBH_TUNE_MAX_TRIALS),

@@ -88,8 +88,12 @@ typedef struct nbh_config {
     int32_t stack_cap;     /* entries of each vote group's shared-memory stack, 64..256, a
                               multiple of 8 (0: 256); trees deeper than (cap - 8) / 7 + 1
                               levels take the per-level walk */
-    int32_t build_phases;  /* octree insertion launches: 1 (one pass) or 3 (0: 3) */
-    int32_t reserved[5];
+    int32_t build_phases;  /* octree insertion launches: 1 (one pass), 3 or 5 (0: 5) */
+    int32_t build_buckets; /* 1 (or 0, the default): with 3 or 5 phases the lock phases
+                              insert a 1/16 sample of the bodies and every other body joins
+                              the subtree of the sample-tree slot it descends to, built by one
+                              warp without locks (the same tree); 2: lock insertion only */
+    int32_t reserved[4];
 } nbh_config;
 
 /* Fills *cfg with the defaults: theta 0.5, eps 0.05, dt 0.025, G 1, pool 2.0,
@@ -233,7 +237,8 @@ int nbh_diagnostics(nbh_sim* sim, int32_t flags, nbh_diag* out, int32_t nout);
  * geometry).  On the loaded universes at their current positions it times every force
  * geometry (threads per block 64 / 128 / 256 x stack capacities from the smallest the tree's
  * depth allows, with 2 levels of headroom, to 256) as side-effect-free force launches that
- * write a scratch buffer, and the tree stages with 1 and 3 insertion phases, then keeps the
+ * write a scratch buffer, and the tree stages with 1, 3 and 5 lock insertion phases and with
+ * 3 and 5 phases completed by bucketed subtrees (build_buckets), then keeps the
  * fastest of each for later steps.  Neither choice changes any result: the walk order, the
  * arithmetic and the tree are the same for every geometry.  flags: 0.  Body state and the
  * step counter are left as they were. */
@@ -242,6 +247,7 @@ typedef struct nbh_tune {
     int32_t force_threads;         /* chosen */
     int32_t stack_cap;             /* chosen */
     int32_t build_phases;          /* chosen */
+    int32_t build_buckets;         /* chosen: 1 bucketed completion, 2 lock insertion only */
     int32_t max_depth;             /* tree depth the stack capacities were fitted to */
     float   ms_force;              /* force launch of the choice */
     float   ms_force_before;       /* force launch of the geometry in place before */
@@ -250,7 +256,7 @@ typedef struct nbh_tune {
     int32_t trials;                /* entries used below */
     int32_t trial_kind[NBH_TUNE_MAX_TRIALS];    /* 0 force, 1 tree */
     int32_t trial_a[NBH_TUNE_MAX_TRIALS];       /* threads, or insertion phases */
-    int32_t trial_b[NBH_TUNE_MAX_TRIALS];       /* stack capacity (force) */
+    int32_t trial_b[NBH_TUNE_MAX_TRIALS];       /* stack capacity (force), or bucketed (tree) */
     float   trial_ms[NBH_TUNE_MAX_TRIALS];      /* mean of 3 timed launches after 1 warm-up */
 } nbh_tune;
 int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out);

@@ -21,7 +21,7 @@ def test_autotune_choice_changes_no_result():
     t = b.autotune()
     after = b.stats()
     assert after["steps"] == before["steps"] and after["max_depth"] == before["max_depth"]
-    assert t["force_threads"] in (64, 128, 256) and 64 <= t["stack_cap"] <= 256 and t["build_phases"] in (1, 3)
+    assert t["force_threads"] in (64, 128, 256) and 64 <= t["stack_cap"] <= 256 and t["build_phases"] in (1, 3, 5)
     assert t["max_depth"] == before["max_depth"]
     assert (t["stack_cap"] - 8) // 7 + 1 >= t["max_depth"] or t["stack_cap"] == 256
     assert any(tr["kind"] == "force" for tr in t["trials"]) and any(tr["kind"] == "tree" for tr in t["trials"])
@@ -55,11 +55,12 @@ def test_force_geometries_match_oracle(vote, threads, cap):
     assert rel.max() <= 1e-4, rel.max()
 
 
-def test_single_pass_build_gives_the_same_tree():
+@pytest.mark.parametrize("phases,buckets", [(1, 2), (5, 2), (3, 1), (5, 1)])
+def test_phase_schedules_give_the_same_tree(phases, buckets):
     n = 30000
     arrs = plummer(n, seed=83)
-    a = gpu_sim(theta=0.5, eps=0.05, dt=0.01, build_phases=1)
-    b = gpu_sim(theta=0.5, eps=0.05, dt=0.01, build_phases=3)
+    a = gpu_sim(theta=0.5, eps=0.05, dt=0.01, build_phases=phases, build_buckets=buckets)
+    b = gpu_sim(theta=0.5, eps=0.05, dt=0.01, build_phases=3, build_buckets=2)
     a.load(*arrs)
     b.load(*arrs)
     a.step(2)
