@@ -163,6 +163,51 @@ def workload(args, seed):
     return tuple(np.concatenate([p[k] for p in parts]) for k in range(7)), counts
 
 
+def shard_universes(counts, world, rank):
+    """Universes of a batch for one rank: greedy balancing of sum N log N (largest first,
+    each to the least loaded rank; deterministic).  Ranks share no data, so the batch
+    shards without a collective on the data path."""
+    import numpy as np
+    counts = np.asarray(counts, dtype=np.int64)
+    cost = counts * np.log2(np.maximum(counts, 2))
+    order = np.argsort(-cost, kind="stable")
+    load = np.zeros(world)
+    owner = np.empty(counts.size, np.int64)
+    for u in order:
+        r = int(np.argmin(load))
+        owner[u] = r
+        load[r] += cost[u]
+    return np.flatnonzero(owner == rank)
+
+
+def select_universes(arrs, counts, keep):
+    """The arrays and counts of the universes `keep` (indices, ascending) of a batch."""
+    import numpy as np
+    offs = np.concatenate([[0], np.cumsum(counts)])
+    idx = np.concatenate([np.arange(offs[u], offs[u + 1]) for u in keep])
+    return tuple(a[idx] for a in arrs), np.asarray(counts)[keep]
+
+
+def reduce_sum(x, dist=None, device="cpu"):
+    """Sum of x over the ranks of the default process group (x itself without one)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def reduce_max(x, dist=None, device="cpu"):
+    """Maximum of x over the ranks of the default process group (x itself without one)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _oracles(arrs, counts, args):
     """One oracle port instance per universe (the port holds a single universe)."""
     import oracle as O
@@ -314,7 +359,13 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    arrs, counts = workload(args, args.seed + rank)
+    if args.workload == "ensemble":
+        # one ensemble for the whole job, its universes sharded across the ranks
+        arrs, counts = workload(args, args.seed)
+        if world > 1:
+            arrs, counts = select_universes(arrs, counts, shard_universes(counts, world, rank))
+    else:
+        arrs, counts = workload(args, args.seed + rank)     # an independent replica per rank
     n = arrs[0].size
     precise = WORKLOADS[args.workload]["precise"]
 
@@ -334,11 +385,7 @@ def main():
             flush.zero_()
 
     def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(x, dist, dev)
 
     # ---- plain fixed theta: warm-up, error of one step, timed steps ---------------------
     sim = new_sim()
@@ -454,7 +501,7 @@ def main():
         lms = max_over_ranks(sum(lstep_ms) / len(lstep_ms))
         th = LR.read_theta(ls)
         learned = {
-            "ms_per_step": lms / world, "speedup_vs_plain": ms / lms,
+            "ms_per_step": lms / (world if args.workload != "ensemble" else 1), "speedup_vs_plain": ms / lms,
             "force_error": lerr, "p99_vs_plain": lerr["p99"] / force_error["p99"],
             "equal_or_lower_p99": bool(lerr["p99"] <= force_error["p99"]),
             "interactions_per_step": int(lst["interactions"]),
@@ -462,7 +509,8 @@ def main():
             "theta_mean": float(th.mean()), "theta_p10": float(np.percentile(th, 10)),
             "theta_p90": float(np.percentile(th, 90)),
             "model": os.path.relpath(model_path, ROOT),
-            "gint_per_s": int(lst["interactions"]) * world / (lms * 1e-3) / 1e9,
+            "gint_per_s": int(lst["interactions"]) * (world if args.workload != "ensemble" else 1)
+                          / (lms * 1e-3) / 1e9,
         }
         ls.close()
 
@@ -477,14 +525,20 @@ def main():
                          % (k, n, args.workload, "; one port instance per universe" if counts is not None else ""),
                "interactions_per_step": cpu_inter}
 
+    # replicas (one independent universe per rank): time per universe-step of the job;
+    # a sharded ensemble: the job's step takes the slowest rank's time
+    replicas = args.workload != "ensemble"
+    div = world if replicas else 1
+    job_inter = interactions * world if replicas else reduce_sum(interactions, dist, dev)
     if rank == 0:
         line = {
-            "metric": METRIC, "value": ms / world, "unit": "ms/step", "n_gpus": world,
+            "metric": METRIC, "value": ms / div, "unit": "ms/step", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic: seeded %s, %d bodies per replica" % (WORKLOADS[args.workload]["what"], n),
+            "scaling": "weak" if replicas else "strong", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded %s, %d bodies %s" % (WORKLOADS[args.workload]["what"], n,
+                                                            "per replica" if replicas else "on rank 0's shard"),
             "config": _config(args, n, counts),
-            "gint_per_s": interactions * world / (ms * 1e-3) / 1e9,
+            "gint_per_s": job_inter / (ms * 1e-3) / 1e9,
             "gint_per_s_force_only": inter_ts / (force_ms * 1e-3) / 1e9,
             "interactions_per_step": interactions,
             "max_depth": int(st["max_depth"]), "cells": cells,
@@ -496,7 +550,7 @@ def main():
             "autotune": None if tune is None else {k: tune[k] for k in (
                 "force_threads", "stack_cap", "build_phases", "build_buckets", "max_depth", "ms_force", "ms_force_before",
                 "ms_tree", "ms_tree_before")},
-            "e2e": {"value": e2e_ms / world, "unit": "ms/step", "h2d_bytes_per_step": 36 * n,
+            "e2e": {"value": e2e_ms / div, "unit": "ms/step", "h2d_bytes_per_step": 36 * n,
                     "d2h_bytes_per_step": 36 * n, "wall_ms_per_step": wall_ms,
                     "path": "nbh_write (pinned host) -> nbh_step -> nbh_read (pinned host)"},
             "gpu_launches": GRAPH_LAUNCHES * args.steps,

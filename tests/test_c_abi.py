@@ -38,7 +38,33 @@ def test_config_struct_layout_matches_header():
     assert (cfg.theta, cfg.G, cfg.pool_factor) == (0.5, 1.0, 2.0)
     assert cfg.eps == pytest.approx(0.05) and cfg.dt == pytest.approx(0.025)
     assert cfg.vote_width == 64 and cfg.arith == L.NBH_ARITH_FMA and cfg.use_graph == 1
-    assert C.sizeof(L.NbhConfig) == 4 * (2 + 7 + 5 + 8)
+    assert C.sizeof(L.NbhConfig) == 4 * (2 + 7 + 9 + 4)
+
+
+def test_struct_layouts_match_the_c_compiler(tmp_path):
+    """sizeof and field offsets of every struct in include/nbh.h, as gcc lays them out, equal
+    the ctypes mirrors the binding uses."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    structs = {"nbh_config": L.NbhConfig, "nbh_stats": L.NbhStats, "nbh_diag": L.NbhDiag, "nbh_tune": L.NbhTune}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "nbh.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in py._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                         check=True).stdout.splitlines())
+    for cname, py in structs.items():
+        assert int(out[cname]) == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert int(out["%s.%s" % (cname, fname)]) == getattr(py, fname).offset, (cname, fname)
 
 
 def test_mlp_constants_match_header_and_network_shape():
