@@ -2,6 +2,8 @@
 
   python gpu-nbody_gb300/nbh/train_theta.py [--n 1048576] [--out PATH]
 
+  python gpu-nbody_gb300/nbh/train_theta.py --study     # ceiling of a per-body angle
+
 Training data: Plummer spheres (scale radius 1, mass 1) of n bodies, two seeds, each at
 its initial state and after a few steps; per snapshot nbh.learned.collect() probes the
 force at the angle grid on sampled bodies and measures the error against the FP64 direct
@@ -69,6 +71,40 @@ def evaluate(arrs, model, theta=0.5, eps=0.05, dt=0.01, nsample=4096, warm=3, cy
     return out
 
 
+def study(n=1 << 20, seed=2024, grid=(0.4, 0.45, 0.5, 0.55, 0.6, 0.7, 0.8, 0.9, 1.0, 1.1, 1.2), fracs=(0.5, 0.7, 1.0),
+          device=0, nsample=4096):
+    """Ceiling of a per-body opening angle on a Plummer sphere: every body's relative force
+    error at each fixed angle of `grid` (against a theta = 0.05 walk, itself checked against
+    the FP64 direct sum on `nsample` bodies), then the walk with each body's own ideal angle
+    (the largest grid angle, monotone, whose error stays within frac * p99 of theta = 0.5),
+    whose interactions and p99 are compared with the fixed angles'.  Returns a dict."""
+    arrs = U.PlummerUniverseGenerator(seed=seed).arrays(n)
+    out = {"n": n, "fixed": {}, "ideal": {}}
+    with nbh.Simulation(theta=0.5, eps=0.05, dt=0.01, device=device) as s:
+        s.load(*arrs)
+        s.step(3)
+        idx = np.sort(np.random.default_rng(17).choice(n, min(nsample, n), replace=False)).astype(np.int32)
+        f64 = s.direct_f64(idx)
+        rx, ry, rz, _, ri = LR.probe(s, np.full(n, 0.05, np.float32))
+        e_ref = LR.rel_error(rx[idx], ry[idx], rz[idx], *f64)
+        out["reference_walk"] = {"theta": 0.05, "interactions": ri, "p99_vs_fp64": float(np.percentile(e_ref, 99))}
+        E = []
+        for th in grid:
+            ax, ay, az, _, it = LR.probe(s, np.full(n, th, np.float32))
+            e = LR.rel_error(ax, ay, az, rx, ry, rz)
+            E.append(e)
+            out["fixed"]["%.2f" % th] = {"interactions": it, "p50": float(np.median(e)), "p99": float(np.percentile(e, 99))}
+        E = np.stack(E)
+        p99 = out["fixed"]["0.50"]["p99"]
+        for frac in fracs:
+            T = np.exp(LR.theta_target(E, frac * p99, grid=tuple(grid), floor=0.3))
+            ax, ay, az, _, it = LR.probe(s, T.astype(np.float32))
+            e = LR.rel_error(ax, ay, az, rx, ry, rz)
+            out["ideal"]["%.1f" % frac] = {"interactions": it, "p50": float(np.median(e)), "p99": float(np.percentile(e, 99)),
+                                          "theta_mean": float(T.mean())}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=1 << 20)
@@ -77,7 +113,22 @@ def main():
     ap.add_argument("--iters", type=int, default=1500)
     ap.add_argument("--every", type=int, default=4, help="steps between model evaluations")
     ap.add_argument("--group", type=int, default=0, help="1: each vote group walks with its smallest angle")
+    ap.add_argument("--study", action="store_true", help="measure the ceiling of a per-body angle and exit")
     args = ap.parse_args()
+    if args.study:
+        r = study(n=args.n)
+        print(json.dumps(r, indent=1))
+        fx = r["fixed"]
+        for frac, v in r["ideal"].items():
+            # the fixed angle with the same p99, by log-interpolating the fixed-angle curve
+            ths = sorted(fx, key=float)
+            p = [fx[t]["p99"] for t in ths]
+            it = [fx[t]["interactions"] for t in ths]
+            eq = float(np.interp(np.log(v["p99"]), np.log(p), np.log(it)))
+            print("ideal per-body angle at tau = %s x p99(0.5): %.3e interactions, p99 %.2e; a fixed angle "
+                  "with that p99: %.3e interactions (gain %.2fx)" % (frac, v["interactions"], v["p99"], np.exp(eq),
+                                                                      np.exp(eq) / v["interactions"]))
+        return
     t0 = time.time()
     rng = np.random.default_rng(1)
     Es, Fs = [], []
