@@ -918,12 +918,14 @@ int nbh_diagnostics(nbh_sim* sim, int32_t flags, nbh_diag* out, int32_t nout) {
 int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
     if (!sim || !out) return NBH_ERR_INVALID;
     if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_autotune before nbh_load");
-    if (flags != 0) return fail(sim, NBH_ERR_INVALID, "flags must be 0");
+    if (flags & ~NBH_TUNE_VOTE) return fail(sim, NBH_ERR_INVALID, "unknown flags");
+    if ((flags & NBH_TUNE_VOTE) && sim->cfg.arith == NBH_ARITH_REFERENCE)
+        return fail(sim, NBH_ERR_INVALID, "vote-width tuning needs FMA arithmetic");
     CK(cudaSetDevice(sim->device));
     cudaStream_t s = sim->stream;
     std::memset(out, 0, sizeof(*out));
     const bool ref = sim->cfg.arith == NBH_ARITH_REFERENCE;
-    const int vote = sim->cfg.vote_width;
+    const int vote_before = sim->cfg.vote_width;
     // snapshot of the device state word: restored at the end, so the step counter, the
     // depth and the counters read as before
     DevState saved;
@@ -961,11 +963,12 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
         *ms = tot / 3.0f;
         return cudaGetLastError();
     };
-    auto add_trial = [&](int kind, int x, int y, float ms) {
+    auto add_trial = [&](int kind, int x, int y, int v, float ms) {
         if (out->trials < NBH_TUNE_MAX_TRIALS) {
             out->trial_kind[out->trials] = kind;
             out->trial_a[out->trials] = x;
             out->trial_b[out->trials] = y;
+            out->trial_vote[out->trials] = v;
             out->trial_ms[out->trials] = ms;
             ++out->trials;
         }
@@ -988,9 +991,13 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
     std::sort(geo.begin(), geo.end());
     geo.erase(std::unique(geo.begin(), geo.end()), geo.end());
     float best_ms = 1e30f;
-    int best_t = sim->force_threads, best_c = sim->stack_cap;
+    int best_t = sim->force_threads, best_c = sim->stack_cap, best_v = vote_before;
     cudaError_t err = cudaSuccess;
+    std::vector<int> votes{vote_before};
+    if (flags & NBH_TUNE_VOTE) votes = {32, 64};
+    for (const int vote : votes)
     for (const auto& g : geo) {
+        if (err != cudaSuccess) break;
         if (!force_geometry_valid(vote, g.first, g.second)) continue;
         int occ = 0;
         if ((err = static_cast<cudaError_t>(occupancy_force(vote, ref, g.first, g.second, &occ))) != cudaSuccess) break;
@@ -1003,12 +1010,14 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
         float ms = 0.0f;
         err = timed([&] { launch_force(q, vote, ref, false, grid, g.first, s); }, &ms);
         if (err != cudaSuccess) break;
-        add_trial(0, g.first, g.second, ms);
-        if (g.first == sim->force_threads && g.second == sim->stack_cap) out->ms_force_before = ms;
+        add_trial(0, g.first, g.second, vote, ms);
+        if (vote == vote_before && g.first == sim->force_threads && g.second == sim->stack_cap)
+            out->ms_force_before = ms;
         if (ms < best_ms) {
             best_ms = ms;
             best_t = g.first;
             best_c = g.second;
+            best_v = vote;
         }
     }
     // tree stages: one lock pass; three or five lock phases; three or five with the bucketed
@@ -1028,7 +1037,7 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
         float ms = 0.0f;
         err = timed([&] { enqueue_tree(sim, p); }, &ms);
         if (err != cudaSuccess) break;
-        add_trial(1, tc[0], tc[1], ms);
+        add_trial(1, tc[0], tc[1], 0, ms);
         if (tc[0] == phases_before && (tc[1] != 0) == (buckets_before && phases_before != 1)) out->ms_tree_before = ms;
         if (ms < best_tree) {
             best_tree = ms;
@@ -1050,11 +1059,13 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
     CK(cudaStreamSynchronize(s));
     sim->force_threads = best_t;
     sim->stack_cap = best_c;
+    sim->cfg.vote_width = best_v;
     sim->build_phases = best_ph;
     sim->build_buckets = best_bk;
     if ((e = set_geometry(sim))) return e;
     drop_graph(sim);
     out->force_threads = best_t;
+    out->vote_width = best_v;
     out->stack_cap = best_c;
     out->build_phases = best_ph;
     out->build_buckets = best_bk ? 1 : 2;

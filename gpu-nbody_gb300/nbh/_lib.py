@@ -70,17 +70,21 @@ class NbhDiag(C.Structure):
 
 
 NBH_DIAG_POTENTIAL = 1
-NBH_TUNE_MAX_TRIALS = 16
+NBH_TUNE_VOTE = 1
+NBH_TUNE_MAX_TRIALS = 32
 
 
 class NbhTune(C.Structure):
     _fields_ = [
         ("force_threads", C.c_int32), ("stack_cap", C.c_int32), ("build_phases", C.c_int32),
-        ("build_buckets", C.c_int32), ("max_depth", C.c_int32), ("ms_force", C.c_float), ("ms_force_before", C.c_float),
+        ("build_buckets", C.c_int32), ("vote_width", C.c_int32), ("max_depth", C.c_int32),
+        ("ms_force", C.c_float), ("ms_force_before", C.c_float),
         ("ms_tree", C.c_float), ("ms_tree_before", C.c_float), ("trials", C.c_int32),
         ("trial_kind", C.c_int32 * NBH_TUNE_MAX_TRIALS), ("trial_a", C.c_int32 * NBH_TUNE_MAX_TRIALS),
-        ("trial_b", C.c_int32 * NBH_TUNE_MAX_TRIALS), ("trial_ms", C.c_float * NBH_TUNE_MAX_TRIALS),
+        ("trial_b", C.c_int32 * NBH_TUNE_MAX_TRIALS), ("trial_vote", C.c_int32 * NBH_TUNE_MAX_TRIALS),
+        ("trial_ms", C.c_float * NBH_TUNE_MAX_TRIALS),
     ]
+
 
 _P = C.c_void_p
 _F = C.POINTER(C.c_float)

@@ -176,15 +176,16 @@ class Simulation:
             out.append(r)
         return out
 
-    def autotune(self) -> dict:
+    def autotune(self, vote: bool = False) -> dict:
         """Pick the force launch geometry and the build's insertion phases by timing them on
-        the loaded universes (nbh_autotune); later steps use the choice."""
+        the loaded universes (nbh_autotune); later steps use the choice.  vote=True also
+        times vote widths 32 and 64 (changes the interaction set)."""
         t = L.NbhTune()
-        self._check(self._L.nbh_autotune(self._h, 0, C.byref(t)))
+        self._check(self._L.nbh_autotune(self._h, L.NBH_TUNE_VOTE if vote else 0, C.byref(t)))
         trials = [{"kind": ("force", "tree")[t.trial_kind[k]], "a": t.trial_a[k], "b": t.trial_b[k],
-                   "ms": t.trial_ms[k]} for k in range(t.trials)]
+                   "vote": t.trial_vote[k], "ms": t.trial_ms[k]} for k in range(t.trials)]
         return {"force_threads": t.force_threads, "stack_cap": t.stack_cap, "build_phases": t.build_phases,
-                "build_buckets": t.build_buckets,
+                "build_buckets": t.build_buckets, "vote_width": t.vote_width,
                 "max_depth": t.max_depth, "ms_force": t.ms_force, "ms_force_before": t.ms_force_before,
                 "ms_tree": t.ms_tree, "ms_tree_before": t.ms_tree_before, "trials": trials}
 

@@ -238,16 +238,21 @@ int nbh_diagnostics(nbh_sim* sim, int32_t flags, nbh_diag* out, int32_t nout);
  * geometry (threads per block 64 / 128 / 256 x stack capacities from the smallest the tree's
  * depth allows, with 2 levels of headroom, to 256) as side-effect-free force launches that
  * write a scratch buffer, and the tree stages with 1, 3 and 5 lock insertion phases and with
- * 3 and 5 phases completed by bucketed subtrees (build_buckets), then keeps the
- * fastest of each for later steps.  Neither choice changes any result: the walk order, the
- * arithmetic and the tree are the same for every geometry.  flags: 0.  Body state and the
+ * 3 and 5 phases completed by bucketed subtrees (build_buckets), then keeps the fastest of
+ * each for later steps.  Neither choice changes any result: the walk order, the arithmetic
+ * and the tree are the same for every geometry.  With NBH_TUNE_VOTE (FMA arithmetic only)
+ * it also times vote widths 32 and 64 -- bodies per traversal group: one warp with one or
+ * two bodies per lane -- and keeps the faster; that choice changes the interaction set (a
+ * larger group opens a few more cells), so it is off unless asked for.  Body state and the
  * step counter are left as they were. */
-#define NBH_TUNE_MAX_TRIALS 16
+#define NBH_TUNE_VOTE 1
+#define NBH_TUNE_MAX_TRIALS 32
 typedef struct nbh_tune {
     int32_t force_threads;         /* chosen */
     int32_t stack_cap;             /* chosen */
     int32_t build_phases;          /* chosen */
     int32_t build_buckets;         /* chosen: 1 bucketed completion, 2 lock insertion only */
+    int32_t vote_width;            /* chosen (the sim's own unless NBH_TUNE_VOTE) */
     int32_t max_depth;             /* tree depth the stack capacities were fitted to */
     float   ms_force;              /* force launch of the choice */
     float   ms_force_before;       /* force launch of the geometry in place before */
@@ -257,6 +262,7 @@ typedef struct nbh_tune {
     int32_t trial_kind[NBH_TUNE_MAX_TRIALS];    /* 0 force, 1 tree */
     int32_t trial_a[NBH_TUNE_MAX_TRIALS];       /* threads, or insertion phases */
     int32_t trial_b[NBH_TUNE_MAX_TRIALS];       /* stack capacity (force), or bucketed (tree) */
+    int32_t trial_vote[NBH_TUNE_MAX_TRIALS];    /* vote width (force) */
     float   trial_ms[NBH_TUNE_MAX_TRIALS];      /* mean of 3 timed launches after 1 warm-up */
 } nbh_tune;
 int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out);

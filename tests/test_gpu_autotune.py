@@ -69,3 +69,32 @@ def test_phase_schedules_give_the_same_tree(phases, buckets):
     sa, sb = a.read(), b.read()
     for k in KEYS:
         np.testing.assert_array_equal(sa[k], sb[k])
+
+
+def test_vote_tuning_picks_a_width_and_stays_parity_clean():
+    """NBH_TUNE_VOTE times vote widths 32 and 64; the chosen width then matches the oracle's
+    groups of that size."""
+    n = 20000
+    arrs = plummer(n, seed=84)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    g.load(*arrs)
+    g.step(1)
+    t = g.autotune(vote=True)
+    assert t["vote_width"] in (32, 64)
+    assert {tr["vote"] for tr in t["trials"] if tr["kind"] == "force"} == {32, 64}
+    before = g.read()
+    o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=t["vote_width"], fma=True)
+    o.load(*[before[k] for k in ("x", "y", "z", "vx", "vy", "vz")], arrs[6])
+    g.step(1)
+    o.step(1)
+    assert g.stats()["interactions"] == o.interactions
+    rel, _ = acc_rel(g.read(), o.state())
+    assert rel.max() <= 1e-4
+
+
+def test_vote_tuning_refused_in_reference_arithmetic():
+    import nbh
+    g = gpu_sim(theta2=1.5, eps2=0.0025, dt=0.025, vote_width=16, arith=nbh.NBH_ARITH_REFERENCE)
+    g.load(*plummer(4096, seed=85))
+    with pytest.raises(nbh.NbhError):
+        g.autotune(vote=True)
