@@ -256,6 +256,26 @@ def test_precise_mode_matches_oracle():
         assert np.abs(gs[k] - os_[k]).max() <= 1e-5 * np.abs(os_[k]).max()
 
 
+def test_precise_mode_keeps_increments_below_an_ulp():
+    """Two light bodies at x = +-1000 drifting at 1e-3 with dt = 1e-3: each step moves them
+    1e-6, below half an FP32 ulp at 1000 (6.1e-5), so plain updates never move them while
+    the Kahan-compensated ones (precise mode) advance them by 1000 steps * 1e-6 = 1e-3."""
+    x = np.array([1000.0, -1000.0], np.float32)
+    z0 = np.zeros(2, np.float32)
+    vx = np.array([1e-3, -1e-3], np.float32)
+    m = np.full(2, 1e-12, np.float32)            # forces ~1e-19: negligible
+    out = {}
+    for precise in (False, True):
+        g = gpu_sim(theta=0.5, eps=0.05, dt=1e-3, precise=precise)
+        g.load(x, z0, z0, vx, z0, z0, m)
+        g.step(1000)
+        out[precise] = g.read()["x"].astype(np.float64)
+        g.close()
+    np.testing.assert_array_equal(out[False], x.astype(np.float64))
+    ulp = np.spacing(np.float32(1000.0))
+    np.testing.assert_allclose(out[True], [1000.0 + 1e-3, -1000.0 - 1e-3], rtol=0, atol=float(ulp))
+
+
 def test_direct_f64_matches_oracle():
     import oracle as O
     n = 30000
