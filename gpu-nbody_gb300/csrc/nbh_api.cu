@@ -266,6 +266,34 @@ bool finite_all(const float* a, int n) {
     return true;
 }
 
+// A device view of n floats of the caller's host memory, when all of [p, p + n) is pinned
+// host memory mapped for the device (checked at both ends; the runtime reports the mapping),
+// else null.  Pageable or unregistered memory takes the staging copies instead, so a kernel
+// never touches host memory the runtime has not mapped.
+const float* mapped_host_view(const float* p, int n) {
+    if (!p || n <= 0) return nullptr;
+    cudaPointerAttributes a0{}, a1{};
+    if (cudaPointerGetAttributes(&a0, p) != cudaSuccess || cudaPointerGetAttributes(&a1, p + (n - 1)) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+        return nullptr;
+    const float* d0 = static_cast<const float*>(a0.devicePointer);
+    const float* d1 = static_cast<const float*>(a1.devicePointer);
+    return d1 - d0 == n - 1 ? d0 : nullptr;
+}
+
+// Device views of up to nine arrays: true when every non-null one is mapped pinned memory.
+bool mapped_host_views(const float* const src[9], int n, HostArrays* h) {
+    for (int k = 0; k < 9; ++k) {
+        h->p[k] = nullptr;
+        if (!src[k]) continue;
+        if (!(h->p[k] = mapped_host_view(src[k], n))) return false;
+    }
+    return true;
+}
+
 int upload_soa(nbh_sim* sim, int n, const float* const src[10]) {
     for (int k = 0; k < 10; ++k) {
         if (!src[k]) continue;
@@ -677,10 +705,17 @@ int nbh_read(nbh_sim* sim, float* x, float* y, float* z, float* vx, float* vy, f
     CK(cudaSetDevice(sim->device));
     const int n = sim->nbody;
     cudaStream_t s = sim->stream;
+    float* dst[9] = {x, y, z, vx, vy, vz, ax, ay, az};
+    HostArrays h;
+    if (mapped_host_views(dst, n, &h)) {       // pinned caller arrays: written in place
+        launch_unpack_host(n, h, sim->node4, sim->vel, sim->acc, std::max(1, (n + 255) / 256), s);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(s));
+        return NBH_OK;
+    }
     launch_unpack(n, sim->staging, sim->node4, sim->vel, sim->acc, std::max(1, std::min((n + 255) / 256, 4 * sim->sms)),
                   s);
     CK(cudaGetLastError());
-    float* dst[9] = {x, y, z, vx, vy, vz, ax, ay, az};
     for (int k = 0; k < 9; ++k)
         if (dst[k])
             CK(cudaMemcpyAsync(dst[k], sim->staging + (size_t)k * n, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
@@ -698,9 +733,16 @@ int nbh_write(nbh_sim* sim, const float* x, const float* y, const float* z, cons
     CK(cudaSetDevice(sim->device));
     const int n = sim->nbody;
     const float* src[10] = {x, y, z, vx, vy, vz, ax, ay, az, nullptr};
+    const int mask = (x ? 1 : 0) | (vx ? 2 : 0) | (ax ? 4 : 0);
+    HostArrays h;
+    if (mask && mapped_host_views(src, n, &h)) {   // pinned caller arrays: read in place
+        launch_pack_host(n, h, mask, sim->node4, sim->vel, sim->acc, std::max(1, (n + 255) / 256), sim->stream);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(sim->stream));
+        return NBH_OK;
+    }
     int e;
     if ((e = upload_soa(sim, n, src))) return e;
-    const int mask = (x ? 1 : 0) | (vx ? 2 : 0) | (ax ? 4 : 0);
     if (mask)
         launch_pack(n, sim->staging, mask, sim->node4, sim->vel, sim->acc,
                     std::max(1, std::min((n + 255) / 256, 4 * sim->sms)), sim->stream);

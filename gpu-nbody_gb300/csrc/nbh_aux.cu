@@ -3,6 +3,8 @@
 #include "nbh_common.cuh"
 #include "nbh_kernels.h"
 
+#include <cstdint>
+
 namespace nbh {
 
 // -------------------------------------------------------------------------------------
@@ -73,6 +75,107 @@ __global__ void unpack_kernel(int n, float* __restrict__ soa, const float4* node
         X[i] = q.x; X[n + i] = q.y; X[2 * n + i] = q.z;
         X[3 * n + i] = v.x; X[4 * n + i] = v.y; X[5 * n + i] = v.z;
         X[6 * n + i] = a.x; X[7 * n + i] = a.y; X[8 * n + i] = a.z;
+    }
+}
+
+// The same as pack / unpack, reading or writing the caller's pinned host arrays directly
+// (device-mapped pinned memory over NVLink-C2C): one launch in place of up to nine copies
+// and a staging pass.  Null entries are skipped.  Each thread moves four consecutive bodies
+// with 16-byte host accesses when every array is 16-byte aligned (vec4), else one body.
+__global__ void pack_host_kernel(int n, HostArrays h, int mask, bool vec4, float4* node4, float4* vel,
+                                 float4* acc) {
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (vec4) {
+        for (int i4 = t0; 4 * i4 < n; i4 += stride) {
+            const int i = 4 * i4;
+            if (i + 3 >= n) {                         // ragged end: one body at a time
+                for (int j = i; j < n; ++j) {
+                    if (mask & 1) { float4 q = node4[j]; q.x = h.p[0][j]; q.y = h.p[1][j]; q.z = h.p[2][j]; node4[j] = q; }
+                    if (mask & 2) vel[j] = make_float4(h.p[3][j], h.p[4][j], h.p[5][j], 0.f);
+                    if (mask & 4) acc[j] = make_float4(h.p[6][j], h.p[7][j], h.p[8][j], 0.f);
+                }
+                continue;
+            }
+            if (mask & 1) {
+                const float4 X = reinterpret_cast<const float4*>(h.p[0])[i4];
+                const float4 Y = reinterpret_cast<const float4*>(h.p[1])[i4];
+                const float4 Z = reinterpret_cast<const float4*>(h.p[2])[i4];
+                const float xs[4] = {X.x, X.y, X.z, X.w}, ys[4] = {Y.x, Y.y, Y.z, Y.w}, zs[4] = {Z.x, Z.y, Z.z, Z.w};
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    float4 q = node4[i + j];
+                    q.x = xs[j]; q.y = ys[j]; q.z = zs[j];
+                    node4[i + j] = q;
+                }
+            }
+#pragma unroll
+            for (int g = 0; g < 2; ++g) {
+                if (!(mask & (2 << g))) continue;
+                const float4 X = reinterpret_cast<const float4*>(h.p[3 + 3 * g])[i4];
+                const float4 Y = reinterpret_cast<const float4*>(h.p[4 + 3 * g])[i4];
+                const float4 Z = reinterpret_cast<const float4*>(h.p[5 + 3 * g])[i4];
+                float4* out = g == 0 ? vel : acc;
+                out[i] = make_float4(X.x, Y.x, Z.x, 0.f);
+                out[i + 1] = make_float4(X.y, Y.y, Z.y, 0.f);
+                out[i + 2] = make_float4(X.z, Y.z, Z.z, 0.f);
+                out[i + 3] = make_float4(X.w, Y.w, Z.w, 0.f);
+            }
+        }
+        return;
+    }
+    for (int i = t0; i < n; i += stride) {
+        if (mask & 1) {
+            float4 q = node4[i];
+            q.x = h.p[0][i]; q.y = h.p[1][i]; q.z = h.p[2][i];
+            node4[i] = q;
+        }
+        if (mask & 2) vel[i] = make_float4(h.p[3][i], h.p[4][i], h.p[5][i], 0.f);
+        if (mask & 4) acc[i] = make_float4(h.p[6][i], h.p[7][i], h.p[8][i], 0.f);
+    }
+}
+
+__global__ void unpack_host_kernel(int n, HostArrays h, bool vec4, const float4* node4, const float4* vel,
+                                   const float4* acc) {
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (vec4) {
+        for (int i4 = t0; 4 * i4 < n; i4 += stride) {
+            const int i = 4 * i4;
+            if (i + 3 >= n) {
+                for (int j = i; j < n; ++j) {
+                    const float4 q = node4[j], v = vel[j], a = acc[j];
+                    const float vals[9] = {q.x, q.y, q.z, v.x, v.y, v.z, a.x, a.y, a.z};
+#pragma unroll
+                    for (int k = 0; k < 9; ++k)
+                        if (h.p[k]) const_cast<float*>(h.p[k])[j] = vals[k];
+                }
+                continue;
+            }
+            float4 q[4], v[4], a[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                q[j] = node4[i + j];
+                v[j] = vel[i + j];
+                a[j] = acc[i + j];
+            }
+            const float4 out[9] = {make_float4(q[0].x, q[1].x, q[2].x, q[3].x), make_float4(q[0].y, q[1].y, q[2].y, q[3].y),
+                                   make_float4(q[0].z, q[1].z, q[2].z, q[3].z), make_float4(v[0].x, v[1].x, v[2].x, v[3].x),
+                                   make_float4(v[0].y, v[1].y, v[2].y, v[3].y), make_float4(v[0].z, v[1].z, v[2].z, v[3].z),
+                                   make_float4(a[0].x, a[1].x, a[2].x, a[3].x), make_float4(a[0].y, a[1].y, a[2].y, a[3].y),
+                                   make_float4(a[0].z, a[1].z, a[2].z, a[3].z)};
+#pragma unroll
+            for (int k = 0; k < 9; ++k)
+                if (h.p[k]) reinterpret_cast<float4*>(const_cast<float*>(h.p[k]))[i4] = out[k];
+        }
+        return;
+    }
+    for (int i = t0; i < n; i += stride) {
+        const float4 q = node4[i], v = vel[i], a = acc[i];
+        const float vals[9] = {q.x, q.y, q.z, v.x, v.y, v.z, a.x, a.y, a.z};
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+            if (h.p[k]) const_cast<float*>(h.p[k])[i] = vals[k];
     }
 }
 
@@ -193,6 +296,21 @@ void launch_pack(int n, const float* soa, int mask, float4* node4, float4* vel, 
 void launch_unpack(int n, float* soa, const float4* node4, const float4* vel, const float4* acc, int grid,
                    cudaStream_t s) {
     unpack_kernel<<<grid, 256, 0, s>>>(n, soa, node4, vel, acc);
+}
+static bool aligned16(const HostArrays& h) {
+    for (const float* q : h.p)
+        if (q && (reinterpret_cast<uintptr_t>(q) & 15)) return false;
+    return true;
+}
+void launch_pack_host(int n, const HostArrays& h, int mask, float4* node4, float4* vel, float4* acc, int grid,
+                      cudaStream_t s) {
+    const bool v4 = aligned16(h);
+    pack_host_kernel<<<v4 ? (grid + 3) / 4 : grid, 256, 0, s>>>(n, h, mask, v4, node4, vel, acc);
+}
+void launch_unpack_host(int n, const HostArrays& h, const float4* node4, const float4* vel, const float4* acc,
+                        int grid, cudaStream_t s) {
+    const bool v4 = aligned16(h);
+    unpack_host_kernel<<<v4 ? (grid + 3) / 4 : grid, 256, 0, s>>>(n, h, v4, node4, vel, acc);
 }
 void launch_export4(int n, const float4* node4, const float4* vel, float4* pos4, float4* vel4, int grid,
                     cudaStream_t s) {

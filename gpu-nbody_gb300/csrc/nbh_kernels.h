@@ -22,6 +22,14 @@ void launch_pack(int n, const float* soa, int mask, float4* node4, float4* vel, 
                  cudaStream_t s);
 void launch_unpack(int n, float* soa, const float4* node4, const float4* vel, const float4* acc, int grid,
                    cudaStream_t s);
+// Device views of the caller's pinned host arrays (x y z vx vy vz ax ay az; null = absent).
+struct HostArrays {
+    const float* p[9];
+};
+void launch_pack_host(int n, const HostArrays& h, int mask, float4* node4, float4* vel, float4* acc, int grid,
+                      cudaStream_t s);
+void launch_unpack_host(int n, const HostArrays& h, const float4* node4, const float4* vel, const float4* acc,
+                        int grid, cudaStream_t s);
 void launch_export4(int n, const float4* node4, const float4* vel, float4* pos4, float4* vel4, int grid,
                     cudaStream_t s);
 void launch_direct_f64(const float4* node4, int nidx, const int* idx, const int2* range, double eps2, double G,

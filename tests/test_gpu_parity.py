@@ -276,6 +276,36 @@ def test_precise_mode_keeps_increments_below_an_ulp():
     np.testing.assert_allclose(out[True], [1000.0 + 1e-3, -1000.0 - 1e-3], rtol=0, atol=float(ulp))
 
 
+def test_pinned_host_arrays_match_the_staged_path():
+    """nbh_write / nbh_read with pinned host arrays (read and written in place by one kernel)
+    give exactly what pageable arrays (staged copies) give."""
+    torch = pytest.importorskip("torch")
+    n = 30000
+    arrs = plummer(n, seed=91)
+    keys = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az")
+    res = {}
+    for pinned in (False, True):
+        g = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+        g.load(*arrs)
+        g.step(2)
+        st = g.read()
+        if pinned:
+            hin = {k: torch.empty(n, dtype=torch.float32, pin_memory=True).numpy() for k in keys}
+            hout = {k: torch.empty(n, dtype=torch.float32, pin_memory=True).numpy() for k in keys}
+        else:
+            hin = {k: np.empty(n, np.float32) for k in keys}
+            hout = {k: np.empty(n, np.float32) for k in keys}
+        for k in keys:
+            hin[k][:] = st[k] * np.float32(1.0 + 1e-3)    # a modified state to write back
+        g.write(*[hin[k] for k in keys])
+        g.step(1)
+        g.read_into(*[hout[k] for k in keys])
+        res[pinned] = {k: hout[k].copy() for k in keys}
+        g.close()
+    for k in keys:
+        np.testing.assert_array_equal(res[True][k], res[False][k])
+
+
 def test_direct_f64_matches_oracle():
     import oracle as O
     n = 30000
