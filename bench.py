@@ -37,9 +37,18 @@ for _p in (os.path.join(ROOT, "gpu-nbody_gb300"), os.path.join(ROOT, "oracle")):
 
 METRIC = "ms/step at 1M bodies, plain vs learned-theta at equal p99 force error; Gint/s"
 DEFAULT_VOTE = 64                   # libnbh's default vote width (nbh_config_default)
-# Kernels in one fixed-angle step graph at the default geometry: bbox, build (5 insertion
-# phases), link, summarize, sort, force, integrate.
-GRAPH_LAUNCHES = 11
+
+
+def graph_launches(build_phases=5, build_buckets=1):
+    """Kernels in one fixed-angle step graph: bbox, the build's launches, link, summarize,
+    sort, force, integrate.  The build is `build_phases` lock phases, or with the bucketed
+    completion the phases up to the 1/16 sample (2 of 3, 3 of 5) plus locate, alloc,
+    scatter and subtree build."""
+    if build_phases == 1 or build_buckets == 2:
+        build = build_phases
+    else:
+        build = (3 if build_phases == 5 else 2) + 4
+    return 6 + build
 FLOPS_PER_INTERACTION = 20          # 3 sub, 3 fma (d^2+eps^2), rsqrt, 3 mul, 3 fma, ~7 more
 HBM_FALLBACK_GBS = 6800.0
 # DRAM bytes (read + write) of one force launch (vote width 64) on the 1,048,576-body
@@ -553,7 +562,8 @@ def main():
             "e2e": {"value": e2e_ms / div, "unit": "ms/step", "h2d_bytes_per_step": 36 * n,
                     "d2h_bytes_per_step": 36 * n, "wall_ms_per_step": wall_ms,
                     "path": "nbh_write (pinned host) -> nbh_step -> nbh_read (pinned host)"},
-            "gpu_launches": GRAPH_LAUNCHES * args.steps,
+            "gpu_launches": graph_launches(**({"build_phases": tune["build_phases"], "build_buckets": tune["build_buckets"]}
+                                              if tune else {})) * args.steps,
             "clocks": clock_info,
             "cpu_baseline": cpu,
             "learned_theta": learned,
