@@ -57,7 +57,7 @@ struct nbh_sim {
     float* model_prm = nullptr;    // its FP32 parameters (device)
     float* probe_theta = nullptr;  // per-body theta of the last force probe (device)
     float* feat = nullptr;         // features of every body (device, nbody * 12)
-    int nchunks = 0, nwarps = 0, nitems64 = 0;
+    int nchunks = 0, nwarps = 0, nitems64 = 0, nitems128 = 0;
     std::vector<int> h_ubody;
     // launch geometry
     int grid_bbox = 0, grid_sum = 0, grid_sort = 0, grid_force = 0, grid_int = 0;
@@ -165,6 +165,8 @@ StepParams step_params(const nbh_sim* sim) {
     p.warps = sim->warps;
     p.items64 = sim->warps + sim->nwarps;     // stored after the 32-body items
     p.nitems64 = sim->nitems64;
+    p.items128 = p.items64 + sim->nitems64;   // then the 128-body items
+    p.nitems128 = sim->nitems128;
     p.nchunks = sim->nchunks;
     p.nwarps = sim->nwarps;
     p.nbody = sim->nbody;
@@ -488,10 +490,10 @@ int nbh_create(const nbh_config* cfg_in, nbh_sim** out) {
     if (!(cfg.theta >= 0.0f) || !(cfg.eps > 0.0f || cfg.eps2 > 0.0f) || !std::isfinite(cfg.dt) ||
         !std::isfinite(cfg.G) || !(cfg.pool_factor > 0.0f) || !(cfg.theta2 >= 0.0f) || !(cfg.eps2 >= 0.0f))
         return fail(nullptr, NBH_ERR_INVALID, "theta must be >= 0, eps > 0, dt and G finite, pool_factor > 0");
-    if (cfg.vote_width != 16 && cfg.vote_width != 32 && cfg.vote_width != 64)
-        return fail(nullptr, NBH_ERR_INVALID, "vote_width must be 16, 32 or 64");
-    if (cfg.vote_width == 64 && cfg.arith == NBH_ARITH_REFERENCE)
-        return fail(nullptr, NBH_ERR_INVALID, "vote_width 64 takes FMA arithmetic");
+    if (cfg.vote_width != 16 && cfg.vote_width != 32 && cfg.vote_width != 64 && cfg.vote_width != 128)
+        return fail(nullptr, NBH_ERR_INVALID, "vote_width must be 16, 32, 64 or 128");
+    if (cfg.vote_width > 32 && cfg.arith == NBH_ARITH_REFERENCE)
+        return fail(nullptr, NBH_ERR_INVALID, "vote_width 64 and 128 take FMA arithmetic");
     if (cfg.arith != NBH_ARITH_FMA && cfg.arith != NBH_ARITH_REFERENCE)
         return fail(nullptr, NBH_ERR_INVALID, "arith must be NBH_ARITH_FMA or NBH_ARITH_REFERENCE");
     const int threads = cfg.force_threads ? cfg.force_threads : 128;
@@ -592,6 +594,9 @@ int nbh_load_batch(nbh_sim* sim, int32_t nuniv, const int32_t* counts, const flo
     const int nw32 = (int)warps.size();
     for (int u = 0; u < nuniv; ++u)
         for (int s = sim->h_ubody[u]; s < sim->h_ubody[u + 1]; s += 64) warps.push_back(make_int2(s, u));
+    const int nw64 = (int)warps.size() - nw32;
+    for (int u = 0; u < nuniv; ++u)
+        for (int s = sim->h_ubody[u]; s < sim->h_ubody[u + 1]; s += 128) warps.push_back(make_int2(s, u));
     int e;
     if ((e = alloc_for(sim, n, nuniv, nnodes, (int)chunks.size(), (int)warps.size()))) return e;
     sim->nbody = n;
@@ -600,7 +605,8 @@ int nbh_load_batch(nbh_sim* sim, int32_t nuniv, const int32_t* counts, const flo
     sim->ncells = nnodes + 1 - n;
     sim->nchunks = (int)chunks.size();
     sim->nwarps = nw32;
-    sim->nitems64 = (int)warps.size() - nw32;
+    sim->nitems64 = nw64;
+    sim->nitems128 = (int)warps.size() - nw32 - nw64;
     cudaStream_t s = sim->stream;
     CK(cudaMemcpyAsync(sim->ubody, sim->h_ubody.data(), sizeof(int) * (nuniv + 1), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(sim->chunks, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice, s));
@@ -1036,7 +1042,7 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
     int best_t = sim->force_threads, best_c = sim->stack_cap, best_v = vote_before;
     cudaError_t err = cudaSuccess;
     std::vector<int> votes{vote_before};
-    if (flags & NBH_TUNE_VOTE) votes = {32, 64};
+    if (flags & NBH_TUNE_VOTE) votes = {32, 64, 128};
     for (const int vote : votes)
     for (const auto& g : geo) {
         if (err != cudaSuccess) break;

@@ -92,9 +92,11 @@ struct StepParams {
     const int4* chunks;  // (universe, begin, end, 0) body chunks that never span universes
     const int2* warps;   // (first sorted position, universe) of each 32-body work item
     const int2* items64; // the same for 64-body items (vote width 64)
+    const int2* items128;// the same for 128-body items (vote width 128)
     int nchunks;
     int nwarps;
     int nitems64;
+    int nitems128;
     int nbody;
     int nnodes;          // NUMBER_OF_NODES (top of the pool)
     int nuniv;

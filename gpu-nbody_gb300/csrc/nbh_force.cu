@@ -126,8 +126,8 @@ __global__ void __launch_bounds__(kForceThreadsMax) force_kernel(StepParams p) {
     const float4* __restrict__ node4 = p.node4;
     const int* __restrict__ child = p.child;
     const float4* __restrict__ kids4 = p.kids4;
-    const int2* __restrict__ items = BPL == 2 ? p.items64 : p.warps;
-    const int nitems = BPL == 2 ? p.nitems64 : p.nwarps;
+    const int2* __restrict__ items = BPL == 4 ? p.items128 : (BPL == 2 ? p.items64 : p.warps);
+    const int nitems = BPL == 4 ? p.nitems128 : (BPL == 2 ? p.nitems64 : p.nwarps);
     unsigned long long my_inter = 0;
 
     for (;;) {
@@ -382,6 +382,7 @@ static cudaError_t prep_force_w() {
 
 int prepare_force_kernels() {
     cudaError_t e = cudaSuccess, t;
+    if ((t = prep_force_w<128, false>()) != cudaSuccess) e = t;
     if ((t = prep_force_w<64, false>()) != cudaSuccess) e = t;
     if ((t = prep_force_w<32, false>()) != cudaSuccess) e = t;
     if ((t = prep_force_w<32, true>()) != cudaSuccess) e = t;
@@ -400,7 +401,9 @@ int force_fast_max_depth(int cap) { return fast_max_depth(cap); }
 
 void launch_force(const StepParams& p, int vote, bool ref, bool feat, int grid, int threads, cudaStream_t s) {
     const bool pb = p.theta_body != nullptr;
-    if (vote == 64) {
+    if (vote == 128) {
+        launch_force_t<128, false>(p, pb, feat, grid, threads, s);  // FMA arithmetic only
+    } else if (vote == 64) {
         launch_force_t<64, false>(p, pb, feat, grid, threads, s);   // FMA arithmetic only
     } else if (vote == 16) {
         if (ref) launch_force_t<16, true>(p, pb, feat, grid, threads, s);
@@ -414,6 +417,9 @@ void launch_force(const StepParams& p, int vote, bool ref, bool feat, int grid, 
 // Resident blocks per SM of the fixed-angle variant at this geometry (the per-body
 // variants use as many registers or fewer per resident warp budget; their grid is the same).
 int occupancy_force(int vote, bool ref, int threads, int cap, int* blocks_per_sm) {
+    if (vote == 128)
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<128, false, false, false>,
+                                                             threads, force_smem_bytes<128>(threads, cap));
     if (vote == 64)
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<64, false, false, false>,
                                                              threads, force_smem_bytes<64>(threads, cap));

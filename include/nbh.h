@@ -76,8 +76,9 @@ typedef struct nbh_config {
     float   pool_factor;   /* node pool = max(pool_factor*N, 16384) rounded up to 16;
                               the reference uses 2.0 (calculateNumberOfNodes) */
     int32_t vote_width;    /* bodies voting together on opening a cell: 64 (two bodies on
-                              each lane of one warp, default; FMA arithmetic), 32 (one warp)
-                              or 16 (the reference work-group, calculateforce.cl:145) */
+                              each lane of one warp, default; FMA arithmetic), 128 (four per
+                              lane; FMA), 32 (one warp) or 16 (the reference work-group,
+                              calculateforce.cl:145) */
     int32_t arith;         /* NBH_ARITH_FMA or NBH_ARITH_REFERENCE */
     int32_t precise;       /* 1: Kahan-compensated position/velocity updates and FP64
                               extent / root centre of mass; 0: reference arithmetic */
@@ -241,8 +242,8 @@ int nbh_diagnostics(nbh_sim* sim, int32_t flags, nbh_diag* out, int32_t nout);
  * 3 and 5 phases completed by bucketed subtrees (build_buckets), then keeps the fastest of
  * each for later steps.  Neither choice changes any result: the walk order, the arithmetic
  * and the tree are the same for every geometry.  With NBH_TUNE_VOTE (FMA arithmetic only)
- * it also times vote widths 32 and 64 -- bodies per traversal group: one warp with one or
- * two bodies per lane -- and keeps the faster; that choice changes the interaction set (a
+ * it also times vote widths 32, 64 and 128 -- bodies per traversal group: one warp with one,
+ * two or four bodies per lane -- and keeps the fastest; that choice changes the interaction set (a
  * larger group opens a few more cells), so it is off unless asked for.  Body state and the
  * step counter are left as they were. */
 #define NBH_TUNE_VOTE 1

@@ -44,7 +44,7 @@ rb_sim* rb_create(int n, int nn, float theta2, float eps2, float dt, float G,
     s->eps2 = eps2;
     s->dt = dt;
     s->G = G;
-    s->vote = vote < 1 ? 1 : vote;
+    s->vote = vote < 1 ? 1 : (vote > RB_MAXVOTE ? RB_MAXVOTE : vote);
     s->fma = fma;
     s->precise = precise;
     size_t nodes = (size_t)nn + 1;
@@ -338,10 +338,10 @@ int rb_force(rb_sim* s) {
         int lo = g * W, hi = lo + W;
         if (hi > n) hi = n;
         const int cnt = hi - lo;
-        int bidx[64];
-        float px[64], py[64], pz[64], t0[64];
-        float ax[64], ay[64], az[64], eb[64];
-        int inter[64];
+        int bidx[RB_MAXVOTE];
+        float px[RB_MAXVOTE], py[RB_MAXVOTE], pz[RB_MAXVOTE], t0[RB_MAXVOTE];
+        float ax[RB_MAXVOTE], ay[RB_MAXVOTE], az[RB_MAXVOTE], eb[RB_MAXVOTE];
+        int inter[RB_MAXVOTE];
         for (int k = 0; k < cnt; ++k) {
             int b = s->sorted[lo + k];
             bidx[k] = b;
@@ -374,7 +374,7 @@ int rb_force(rb_sim* s) {
                 if (ch >= 0) {
                     const float cxn = s->x[ch], cyn = s->y[ch], czn = s->z[ch], cmn = s->m[ch];
                     int accept = 1;
-                    float dxs[64], dys[64], dzs[64], d2s[64];
+                    float dxs[RB_MAXVOTE], dys[RB_MAXVOTE], dzs[RB_MAXVOTE], d2s[RB_MAXVOTE];
                     for (int k = 0; k < cnt; ++k) {
                         float dx = cxn - px[k], dy = cyn - py[k], dz = czn - pz[k];
                         float d2;

@@ -20,6 +20,7 @@ extern "C" {
 #endif
 
 #define RB_MAXDEPTH 64
+#define RB_MAXVOTE 128              /* largest vote group */
 #define RB_OK 0
 #define RB_ERR_INVALID (-1)
 #define RB_ERR_POOL (-3)

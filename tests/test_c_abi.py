@@ -102,8 +102,8 @@ def test_create_without_gpu_fails_loudly():
 
 
 def test_invalid_config_rejected():
-    for kw in ({"eps": 0.0}, {"vote_width": 8}, {"vote_width": 128}, {"theta": -1.0}, {"pool_factor": 0.0},
-               {"vote_width": 64, "arith": L.NBH_ARITH_REFERENCE}, {"force_threads": 96}, {"stack_cap": 300},
+    for kw in ({"eps": 0.0}, {"vote_width": 8}, {"vote_width": 256}, {"theta": -1.0}, {"pool_factor": 0.0},
+               {"vote_width": 64, "arith": L.NBH_ARITH_REFERENCE}, {"vote_width": 128, "arith": L.NBH_ARITH_REFERENCE}, {"force_threads": 96}, {"stack_cap": 300},
                {"stack_cap": 60}, {"stack_cap": 100}, {"build_phases": 2}, {"build_phases": 4},
                {"build_buckets": 3}, {"build_buckets": -1}):
         with pytest.raises(nbh.NbhError) as ei:

@@ -178,15 +178,15 @@ def test_batch_of_universes_matches_oracle_per_universe():
     assert isinstance(nbh.Simulation, type)
 
 
-@pytest.mark.parametrize("n", [20000, 64, 65, 1])
-def test_vote64_matches_oracle_one_step(n):
-    """Vote width 64 (two bodies per lane): groups of 64 consecutive sorted bodies, the
-    last one ragged; same interactions, same depth-first order, accelerations within the
-    FMA tolerance of the oracle's 64-body groups."""
+@pytest.mark.parametrize("vote,n", [(64, 20000), (64, 64), (64, 65), (64, 1), (128, 20000), (128, 129), (128, 127)])
+def test_vote64_matches_oracle_one_step(vote, n):
+    """Vote widths 64 and 128 (two or four bodies per lane): groups of that many consecutive
+    sorted bodies, the last one ragged; same interactions, same depth-first order,
+    accelerations within the FMA tolerance of the oracle's groups of the same size."""
     arrs = plummer(n, seed=21)
-    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=64)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=vote)
     g.load(*arrs)
-    o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=64, fma=True)
+    o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=vote, fma=True)
     o.load(*arrs)
     g.step(2)
     o.step(2)
@@ -200,19 +200,21 @@ def test_vote64_matches_oracle_one_step(n):
         assert np.abs(gs[k] - os_[k]).max() <= 1e-5 * max(1.0, np.abs(os_[k]).max())
 
 
-def test_vote64_batch_of_universes():
-    """Vote width 64 over uneven universes: items never straddle a universe boundary."""
+@pytest.mark.parametrize("vote", [64, 128])
+def test_vote64_batch_of_universes(vote):
+    """Vote widths 64 and 128 over uneven universes: items never straddle a universe
+    boundary."""
     from nbh import universe as U
-    counts = [1024, 33, 5000, 1, 64, 65, 127]
+    counts = [1024, 33, 5000, 1, 64, 65, 127, 129]
     parts = [U.PlummerUniverseGenerator(seed=60 + i).arrays(c) for i, c in enumerate(counts)]
     cat = [np.concatenate([p[k] for p in parts]) for k in range(7)]
-    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=64)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=vote)
     g.load_batch(counts, *cat)
     g.step(2)
     gs = g.read()
     total, off = 0, 0
     for i, c in enumerate(counts):
-        o = oracle_for(c, theta=0.5, eps=0.05, dt=0.01, vote=64, fma=True)
+        o = oracle_for(c, theta=0.5, eps=0.05, dt=0.01, vote=vote, fma=True)
         o.load(*parts[i])
         o.step(2)
         rel, _ = acc_rel({k: gs[k][off:off + c] for k in KEYS}, o.state())
