@@ -53,6 +53,7 @@ struct nbh_sim {
     bool build_buckets = true;     // lock phases insert a 1/16 sample, the rest is built per slot
     int4* buckets = nullptr;       // bucketed build: nbody records
     int* bwork = nullptr;          // bucketed build: 2 * nbody entries
+    unsigned char* bstack = nullptr;   // bucketed build: per-warp task stacks
     ThetaDev* model = nullptr;     // installed model (device)
     float* model_prm = nullptr;    // its FP32 parameters (device)
     float* probe_theta = nullptr;  // per-body theta of the last force probe (device)
@@ -112,7 +113,7 @@ int grow(nbh_sim* sim, T** ptr, size_t count, size_t* cap_unused = nullptr) {
 void free_buffers(nbh_sim* sim) {
     void* ptrs[] = {sim->probe_theta, sim->feat, sim->clevel, sim->probe, sim->loff, sim->kids4, sim->node4, sim->vel, sim->acc, sim->kpos, sim->kvel, sim->child, sim->count,
                     sim->start, sim->arrive, sim->parent, sim->sorted, sim->ubody, sim->ubox,
-                    sim->uradius, sim->chunks, sim->warps, sim->staging, sim->theta_body, sim->buckets, sim->bwork};
+                    sim->uradius, sim->chunks, sim->warps, sim->staging, sim->theta_body, sim->buckets, sim->bwork, sim->bstack};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     sim->kids4 = sim->node4 = sim->vel = sim->acc = sim->kpos = sim->kvel = nullptr;
@@ -128,6 +129,7 @@ void free_buffers(nbh_sim* sim) {
     sim->theta_body = nullptr;
     sim->buckets = nullptr;
     sim->bwork = nullptr;
+    sim->bstack = nullptr;
     sim->cap_body = sim->cap_nodes = sim->cap_univ = sim->cap_chunks = sim->cap_warps = 0;
 }
 
@@ -157,6 +159,7 @@ StepParams step_params(const nbh_sim* sim) {
     p.stack_cap = sim->stack_cap;
     p.buckets = sim->buckets;
     p.bwork = sim->bwork;
+    p.bstack = sim->bstack;
     p.st = sim->st;
     p.ubody = sim->ubody;
     p.ubox = sim->ubox;
@@ -326,6 +329,7 @@ int alloc_for(nbh_sim* sim, int nbody, int nuniv, int nnodes, int nchunks, int n
     if ((e = grow(sim, &sim->probe, (size_t)nbody))) return e;
     if ((e = grow(sim, &sim->buckets, (size_t)nbody))) return e;
     if ((e = grow(sim, &sim->bwork, 2 * (size_t)nbody))) return e;
+    if ((e = grow(sim, &sim->bstack, bucket_stack_bytes(sim->sms)))) return e;
     if ((e = grow(sim, &sim->probe_theta, (size_t)nbody))) return e;
     if ((e = grow(sim, &sim->feat, (size_t)nbody * kMlpIn))) return e;
     if ((e = grow(sim, &sim->start, (size_t)ncells))) return e;

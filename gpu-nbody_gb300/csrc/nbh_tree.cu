@@ -433,10 +433,12 @@ struct SmallTask {
 };
 constexpr int kBucketWarps = 4;
 // Children are pushed largest first, so every stacked sibling holds at most half of its
-// parent's bodies: the stack stays within 7 log2(m) + 8 entries for a bucket of m bodies
-// (155 for m up to 2^21; 43 for the register subtrees of at most 32 bodies).
-constexpr int kBucketStack = 160;
+// parent's bodies: the stack stays within 7 log2(m) + 8 entries for a bucket of m bodies --
+// 225 for any m < 2^31 (the large-bucket stacks live in global memory, one slice per warp
+// of the grid) and 43 for the register subtrees of at most 32 bodies (shared memory).
+constexpr int kBucketStack = 232;
 constexpr int kSmallStack = 48;
+constexpr int kBucketBlocksPerSm = 9;
 
 // Stack position of each child cell among the nc cells pushed now: the largest deepest.
 __device__ __forceinline__ int deeper_rank(int mycnt, int lane) {
@@ -452,7 +454,9 @@ __device__ __forceinline__ int deeper_rank(int mycnt, int lane) {
 // The subtree of the m <= 32 bodies src[lo, lo + m) below a cell of level `level` with the
 // given centre and half-width.  cell >= 0: that cell exists already (its slots are written
 // here); cell < 0: it is taken from the pool with the rest.  Returns the subtree's root cell
-// (or -1 after raising an error).  Whole-warp call.
+// (or -1 after raising an error).  Whole-warp call.  Lanes with a body are grouped by octant
+// (match_any); each group's lowest lane writes its octant's slot -- its own body when alone,
+// else a new cell -- and lanes 0..7 write the empty octants.
 __device__ int build_small(const StepParams& p, const int* __restrict__ src, int lo, int m, int cell, int level,
                            float cx, float cy, float cz, float r, SmallTask* st, int& local_max) {
     const int lane = threadIdx.x & 31;
@@ -468,14 +472,13 @@ __device__ int build_small(const StepParams& p, const int* __restrict__ src, int
     int base = 0, next = 0;
     for (int pass = 0; pass < 2; ++pass) {           // 0: count the cells, 1: build
         int made = 0;
-        if (pass == 1) {
+        if (pass == 1 && next > 0) {
             if (lane == 0) base = atomicSub(&p.st->bottom, next);
             base = __shfl_sync(0xffffffffu, base, 0);
             if (base - next <= nbody) {
                 raise_error(p.st, NBH_ERR_POOL);
                 return -1;
             }
-            made = 0;
         }
         int root = cell;
         if (cell < 0) root = pass == 1 ? base - 1 - made++ : (made++, 0);
@@ -487,40 +490,45 @@ __device__ int build_small(const StepParams& p, const int* __restrict__ src, int
             __syncwarp();
             const bool member = (t.mask >> lane) & 1u;
             const int o = member ? octant(t.cx, t.cy, t.cz, q.x, q.y, q.z) : -1;
-            unsigned mybal = 0;
-#pragma unroll
-            for (int oc = 0; oc < 8; ++oc) {
-                const unsigned bal = __ballot_sync(0xffffffffu, o == oc);
-                if (lane == oc) mybal = bal;
-            }
-            const int mycnt = __popc(mybal);
-            const bool is_cell = lane < 8 && mycnt >= 2;
-            const unsigned balc = __ballot_sync(0xffffffffu, is_cell);
+            const unsigned grp = __match_any_sync(0xffffffffu, o);
+            const bool leader = member && (__ffs(grp) - 1) == lane;
+            const int cnt = __popc(grp);
+            const unsigned balc = __ballot_sync(0xffffffffu, leader && cnt >= 2);
             const int nc = __popc(balc);
             if (nc > 0 && (t.level + 2 > kMaxDepth || top + nc > kSmallStack)) {   // coincident bodies
                 raise_error(p.st, NBH_ERR_DEPTH);
                 return -1;
             }
-            const int deeper = deeper_rank(mycnt, lane);
-            const int single = __shfl_sync(0xffffffffu, b, lane < 8 && mycnt == 1 ? __ffs(mybal) - 1 : 0);
-            if (lane < 8) {
-                int v = kNull;
-                if (mycnt == 1) {
-                    v = single;
-                    local_max = max(local_max, t.level + 1);
-                } else if (mycnt >= 2) {
-                    v = pass == 1 ? base - 1 - made - __popc(balc & lt) : 0;
-                    const float h = t.r * 0.5f;
-                    st[top + deeper] = SmallTask{mybal, v, t.level + 1,
-                                                 __fadd_rn(__fsub_rn(t.cx, h), (lane & 1) ? t.r : 0.0f),
-                                                 __fadd_rn(__fsub_rn(t.cy, h), (lane & 2) ? t.r : 0.0f),
-                                                 __fadd_rn(__fsub_rn(t.cz, h), (lane & 4) ? t.r : 0.0f), h};
+            if (pass == 1) {
+                const unsigned occ = __reduce_or_sync(0xffffffffu, member ? 1u << o : 0u);
+                if (lane < 8 && !((occ >> lane) & 1u)) cell_child(p, t.cell)[lane] = kNull;
+                if (lane == 0) {
+                    p.arrive[t.cell - nbody] = 0;
+                    p.clevel[t.cell - nbody] = t.level;
                 }
-                if (pass == 1) cell_child(p, t.cell)[lane] = v;
             }
-            if (pass == 1 && lane == 0) {
-                p.arrive[t.cell - nbody] = 0;
-                p.clevel[t.cell - nbody] = t.level;
+            // the largest child cell is pushed deepest (popped last); the others above it
+            int pos = 0;
+            if (nc > 1) {
+                const unsigned key = (leader && cnt >= 2) ? ((unsigned)cnt << 5) | (31u - lane) : 0u;
+                const unsigned kmax = __reduce_max_sync(0xffffffffu, key);
+                const int largest = 31 - (int)(kmax & 31u);
+                const unsigned others = balc & ~(1u << largest);
+                pos = lane == largest ? 0 : 1 + __popc(others & lt);
+            }
+            if (leader) {
+                if (cnt == 1) {
+                    if (pass == 1) cell_child(p, t.cell)[o] = b;
+                    local_max = max(local_max, t.level + 1);
+                } else {
+                    const int v = pass == 1 ? base - 1 - made - __popc(balc & lt) : 0;
+                    if (pass == 1) cell_child(p, t.cell)[o] = v;
+                    const float h = t.r * 0.5f;
+                    st[top + pos] = SmallTask{grp, v, t.level + 1,
+                                              __fadd_rn(__fsub_rn(t.cx, h), (o & 1) ? t.r : 0.0f),
+                                              __fadd_rn(__fsub_rn(t.cy, h), (o & 2) ? t.r : 0.0f),
+                                              __fadd_rn(__fsub_rn(t.cz, h), (o & 4) ? t.r : 0.0f), h};
+                }
             }
             made += nc;
             top += nc;
@@ -533,10 +541,10 @@ __device__ int build_small(const StepParams& p, const int* __restrict__ src, int
 }
 
 __global__ void __launch_bounds__(32 * kBucketWarps) bucket_build_kernel(StepParams p) {
-    __shared__ BucketTask stack_all[kBucketWarps][kBucketStack];
     __shared__ SmallTask small_all[kBucketWarps][kSmallStack];
     if (load_status(p.st)) return;
-    BucketTask* stack = stack_all[threadIdx.x >> 5];
+    BucketTask* stack = static_cast<BucketTask*>(p.bstack) +
+                        (size_t)(blockIdx.x * kBucketWarps + (threadIdx.x >> 5)) * kBucketStack;
     SmallTask* sstack = small_all[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -890,7 +898,11 @@ void launch_build(const StepParams& p, int phases, bool buckets, int sms, cudaSt
     const long long cells = (long long)p.nchunks * 16 + p.nuniv;
     bucket_alloc_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(p);
     bucket_scatter_kernel<<<grid_rest, 256, 0, s>>>(p);
-    bucket_build_kernel<<<8 * sms, 32 * kBucketWarps, 0, s>>>(p);
+    bucket_build_kernel<<<kBucketBlocksPerSm * sms, 32 * kBucketWarps, 0, s>>>(p);
+}
+
+size_t bucket_stack_bytes(int sms) {
+    return (size_t)kBucketBlocksPerSm * sms * kBucketWarps * kBucketStack * sizeof(BucketTask);
 }
 void launch_link(const StepParams& p, int grid, cudaStream_t s) {
     link_kernel<<<grid, 256, 0, s>>>(p);

@@ -98,3 +98,29 @@ def test_vote_tuning_refused_in_reference_arithmetic():
     g.load(*plummer(4096, seed=85))
     with pytest.raises(nbh.NbhError):
         g.autotune(vote=True)
+
+
+def test_bucketed_build_when_the_sample_misses_a_cluster():
+    """Input order that defeats the 1/16 sample: every 16th body is spread over a cube, the
+    other 15 in 16 sit in a tiny ball the sample never reaches, so one slot's bucket holds
+    almost every body (the large-bucket path, many levels deep).  The tree and the forces
+    equal the lock-only build's."""
+    n = 16 * 4096
+    r = np.random.default_rng(86)
+    pos = r.uniform(-1, 1, (n, 3)).astype(np.float32)
+    rest = np.arange(n) % 16 != 0
+    pos[rest] = (np.float32(0.31) + r.normal(0, 1e-3, (int(rest.sum()), 3))).astype(np.float32)
+    zero = np.zeros(n, np.float32)
+    m = np.full(n, 1.0 / n, np.float32)
+    arrs = (pos[:, 0].copy(), pos[:, 1].copy(), pos[:, 2].copy(), zero, zero, zero, m)
+    out = {}
+    for buckets in (1, 2):
+        g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, build_phases=5, build_buckets=buckets)
+        g.load(*arrs)
+        g.step(1)
+        out[buckets] = (g.tree()["sorted"], g.read(), g.stats())
+        g.close()
+    np.testing.assert_array_equal(out[1][0], out[2][0])
+    for k in KEYS:
+        np.testing.assert_array_equal(out[1][1][k], out[2][1][k])
+    assert out[1][2]["max_depth"] == out[2][2]["max_depth"] and out[1][2]["status"] == 0
