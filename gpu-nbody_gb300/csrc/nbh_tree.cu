@@ -153,9 +153,13 @@ struct BuildPhase {
 __host__ __device__ constexpr int phase_bodies(BuildPhase ph) {   // per full 256-body chunk
     return ph.ratio > 0 ? 256 / ph.stride - 256 / (ph.stride * ph.ratio) : 256 / ph.stride;
 }
-// Offset inside its chunk of the phase's idx-th body.
-__device__ __forceinline__ int phase_offset(BuildPhase ph, int idx) {
-    return ph.ratio > 0 ? ph.stride * (idx + idx / (ph.ratio - 1) + 1) : ph.stride * idx;
+// Offset inside chunk ci of the phase's idx-th body.  The lattice is rotated by
+// 7 ci mod 16 positions (a bijection of the 256 offsets), so that an input order with a
+// period of 16 (two data sets interleaved 1:15, say) is sampled in every residue class
+// across chunks instead of in one.
+__device__ __forceinline__ int phase_offset(BuildPhase ph, int idx, long long ci) {
+    const int j = ph.ratio > 0 ? ph.stride * (idx + idx / (ph.ratio - 1) + 1) : ph.stride * idx;
+    return (j + (int)((ci * 7) & 15)) & 255;
 }
 constexpr BuildPhase kOnePass[1] = {{1, 0}};
 constexpr BuildPhase kThreePhases[3] = {{256, 0}, {16, 16}, {1, 16}};
@@ -170,7 +174,7 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p, BuildPhase pha
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;   // one body per thread
     if (g < (long long)p.nchunks * per) {
         const int4 ck = p.chunks[g / per];
-        const int b = ck.y + phase_offset(phase, (int)(g % per));
+        const int b = ck.y + phase_offset(phase, (int)(g % per), g / per);
         if (b < ck.z) {
             const int root = p.nnodes - ck.x;
             const float4 rc = p.node4[root];
@@ -314,7 +318,7 @@ __global__ void __launch_bounds__(256) bucket_locate_kernel(StepParams p) {
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= (long long)p.nchunks * per) return;
     const int4 ck = p.chunks[g / per];
-    const int b = ck.y + phase_offset(kBucketBodies, (int)(g % per));
+    const int b = ck.y + phase_offset(kBucketBodies, (int)(g % per), g / per);
     if (b >= ck.z) return;
     const int root = p.nnodes - ck.x;
     const float4 rc = p.node4[root];
@@ -407,7 +411,7 @@ __global__ void __launch_bounds__(256) bucket_scatter_kernel(StepParams p) {
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= (long long)p.nchunks * per) return;
     const int4 ck = p.chunks[g / per];
-    const int b = ck.y + phase_offset(kBucketBodies, (int)(g % per));
+    const int b = ck.y + phase_offset(kBucketBodies, (int)(g % per), g / per);
     if (b >= ck.z) return;
     const int slot = p.parent[b];
     int* bc = bucket_counters(p, p.nbody + (slot >> 3));

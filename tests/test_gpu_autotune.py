@@ -101,14 +101,16 @@ def test_vote_tuning_refused_in_reference_arithmetic():
 
 
 def test_bucketed_build_when_the_sample_misses_a_cluster():
-    """Input order that defeats the 1/16 sample: every 16th body is spread over a cube, the
+    """An input order aliased with the sample lattice (in chunk c of 256 bodies the sample
+    takes the offsets congruent to 7c mod 16): the sampled bodies are spread over a cube, the
     other 15 in 16 sit in a tiny ball the sample never reaches, so one slot's bucket holds
     almost every body (the large-bucket path, many levels deep).  The tree and the forces
     equal the lock-only build's."""
     n = 16 * 4096
     r = np.random.default_rng(86)
     pos = r.uniform(-1, 1, (n, 3)).astype(np.float32)
-    rest = np.arange(n) % 16 != 0
+    i = np.arange(n)
+    rest = ((i % 256) - 7 * (i // 256)) % 16 != 0
     pos[rest] = (np.float32(0.31) + r.normal(0, 1e-3, (int(rest.sum()), 3))).astype(np.float32)
     zero = np.zeros(n, np.float32)
     m = np.full(n, 1.0 / n, np.float32)
