@@ -712,11 +712,10 @@ __global__ void __launch_bounds__(32 * kBucketWarps) bucket_build_kernel(StepPar
 
 // -------------------------------------------------------------------------------------
 // Link: parent[] of every node from the finished tree (one pass over the cells), for the
-// bottom-up summarize.  Keeping it out of the build means an insertion publishes nothing
-// but a slot value.
+// bottom-up summarize, the sort's walk-up and the learned angle's features (a body's leaf
+// cell).  Keeping it out of the build means an insertion publishes nothing but a slot value.
 __global__ void __launch_bounds__(256) link_kernel(StepParams p) {
     if (load_status(p.st)) return;
-    const int nbody = p.nbody;
     const int bottom = p.st->bottom;
     const int stride = gridDim.x * blockDim.x;
     for (int c = bottom + (int)(blockIdx.x * blockDim.x + threadIdx.x); c <= p.nnodes; c += stride) {
@@ -731,11 +730,12 @@ __global__ void __launch_bounds__(256) link_kernel(StepParams p) {
 }
 
 // -------------------------------------------------------------------------------------
-// Summarize (summarizetree.cl:37-178), bottom-up without waiting.  Every body arrives at
-// its parent cell with one atomic; the last of a cell's k children to arrive sums the
-// cell: children compacted to the front in octant order (:77-81), mass and mass-weighted
+// Summarize (summarizetree.cl:37-178), bottom-up without waiting.  One thread per cell
+// starts at the cells whose children are all bodies and sums them at once; every other
+// cell is summed by the last of its cell children to finish (one atomic arrival per cell):
+// children compacted to the front in octant order (:77-81), mass and mass-weighted
 // position summed in that order, centre = sum * (1/mass) (:161-167), body count
-// (:98-118,160); then it arrives at the cell's parent.  The order of the sums is fixed by
+// (:98-118,160); then the climb continues at the cell's parent.  The order of the sums is fixed by
 // the octant order, independent of timing (the reference's depends on which children
 // were ready).  Precise mode sums the roots' centres of mass in FP64.  The last arriver
 // also stores, from the registers it already holds:
@@ -746,17 +746,11 @@ __global__ void __launch_bounds__(256) link_kernel(StepParams p) {
 //     down from the root instead).
 // Arrivals after a write are release atomics and the last arriver acquires, in place of
 // full fences.
-__device__ __forceinline__ int arrive_relaxed(int* p) {
-    int old;
-    asm volatile("atom.relaxed.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
-    return old;
-}
 __device__ __forceinline__ int arrive_acq_rel(int* p) {
     int old;
     asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
     return old;
 }
-__device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
 template <bool REF, bool PRECISE>
 __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
@@ -764,23 +758,22 @@ __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
     const int nbody = p.nbody;
     const int first_root = p.nnodes - p.nuniv + 1;
     const int stride = gridDim.x * blockDim.x;
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbody; b += stride) {
-        int c = p.parent[b];
-        bool from_body = true;
+    const int bottom = ld_relaxed(&p.st->bottom);
+    for (int c0 = bottom + (int)(blockIdx.x * blockDim.x + threadIdx.x); c0 <= p.nnodes; c0 += stride) {
+        int c = c0;
+        bool start = true;
         while (c >= 0) {
             int* ch8 = cell_child(p, c);
             const int4 s0 = reinterpret_cast<const int4*>(ch8)[0];
             const int4 s1 = reinterpret_cast<const int4*>(ch8)[1];
             const int sl[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
-            int k = 0;
+            int kc = 0;                               // cell children
 #pragma unroll
-            for (int j = 0; j < 8; ++j) k += sl[j] >= 0;
-            int* ctr = p.arrive + (c - nbody);
-            if (from_body) {
-                if (arrive_relaxed(ctr) != k - 1) break;
-                fence_acquire();
-            } else {
-                if (arrive_acq_rel(ctr) != k - 1) break;
+            for (int j = 0; j < 8; ++j) kc += sl[j] >= nbody;
+            if (start) {
+                if (kc > 0) break;                    // summed later by its last cell child
+            } else if (arrive_acq_rel(p.arrive + (c - nbody)) != kc - 1) {
+                break;                                // another cell child is still to come
             }
             int used = 0, cnt = 0;
             float cm = 0.0f, sx = 0.0f, sy = 0.0f, sz = 0.0f;
@@ -833,7 +826,7 @@ __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
                 break;
             }
             c = pc;
-            from_body = false;
+            start = false;
         }
     }
 }
