@@ -1046,7 +1046,7 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
     int best_t = sim->force_threads, best_c = sim->stack_cap, best_v = vote_before;
     cudaError_t err = cudaSuccess;
     std::vector<int> votes{vote_before};
-    if (flags & NBH_TUNE_VOTE) votes = {32, 64, 128};
+    if (flags & NBH_TUNE_VOTE) votes = {16, 32, 64, 128};
     for (const int vote : votes)
     for (const auto& g : geo) {
         if (err != cudaSuccess) break;

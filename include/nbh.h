@@ -242,12 +242,12 @@ int nbh_diagnostics(nbh_sim* sim, int32_t flags, nbh_diag* out, int32_t nout);
  * 3 and 5 phases completed by bucketed subtrees (build_buckets), then keeps the fastest of
  * each for later steps.  Neither choice changes any result: the walk order, the arithmetic
  * and the tree are the same for every geometry.  With NBH_TUNE_VOTE (FMA arithmetic only)
- * it also times vote widths 32, 64 and 128 -- bodies per traversal group: one warp with one,
- * two or four bodies per lane -- and keeps the fastest; that choice changes the interaction set (a
+ * it also times vote widths 16, 32, 64 and 128 -- bodies per traversal group: half a warp,
+ * or one warp with one, two or four bodies per lane -- and keeps the fastest; that choice changes the interaction set (a
  * larger group opens a few more cells), so it is off unless asked for.  Body state and the
  * step counter are left as they were. */
 #define NBH_TUNE_VOTE 1
-#define NBH_TUNE_MAX_TRIALS 32
+#define NBH_TUNE_MAX_TRIALS 48
 typedef struct nbh_tune {
     int32_t force_threads;         /* chosen */
     int32_t stack_cap;             /* chosen */

@@ -80,8 +80,8 @@ def test_vote_tuning_picks_a_width_and_stays_parity_clean():
     g.load(*arrs)
     g.step(1)
     t = g.autotune(vote=True)
-    assert t["vote_width"] in (32, 64, 128)
-    assert {tr["vote"] for tr in t["trials"] if tr["kind"] == "force"} == {32, 64, 128}
+    assert t["vote_width"] in (16, 32, 64, 128)
+    assert {tr["vote"] for tr in t["trials"] if tr["kind"] == "force"} == {16, 32, 64, 128}
     before = g.read()
     o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=t["vote_width"], fma=True)
     o.load(*[before[k] for k in ("x", "y", "z", "vx", "vy", "vz")], arrs[6])

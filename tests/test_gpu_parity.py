@@ -308,6 +308,31 @@ def test_pinned_host_arrays_match_the_staged_path():
         np.testing.assert_array_equal(res[True][k], res[False][k])
 
 
+def test_massless_tracers_match_oracle():
+    """A quarter of the bodies carry no mass (tracers).  Cells holding only tracers have no
+    defined centre of mass (0/0, as in the reference's summarize), never pass the opening
+    test and are always opened; the tracers still feel the massive bodies.  Same interactions
+    and forces as the oracle."""
+    n = 20000
+    arrs = list(plummer(n, seed=93))
+    m = arrs[6].copy()
+    m[::4] = 0.0
+    arrs[6] = m
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=32)
+    g.load(*arrs)
+    o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=32, fma=True)
+    o.load(*arrs)
+    g.step(2)
+    o.step(2)
+    gs = g.read()
+    assert g.stats()["status"] == 0
+    assert g.stats()["interactions"] == o.interactions
+    for k in ("ax", "ay", "az", "x", "y", "z"):
+        assert np.isfinite(gs[k]).all(), k
+    rel, _ = acc_rel(gs, o.state())
+    assert rel.max() <= FMA_ACC_REL_MAX, rel.max()
+
+
 def test_direct_f64_matches_oracle():
     import oracle as O
     n = 30000
