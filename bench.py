@@ -338,6 +338,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch geometry")
+    ap.add_argument("--tune-vote", action="store_true",
+                    help="let the autotuner pick the vote width too (changes the interaction set)")
     ap.add_argument("--error-samples", type=int, default=4096)
     ap.add_argument("--profile-only", action="store_true",
                     help="load, warm up and run the timed steps only (for ncu captures)")
@@ -405,7 +407,9 @@ def main():
         sim.step(1)
     # launch geometry picked by the library's autotuner (changes no result); profile runs
     # keep the default geometry so that their launch lists hold only the step's kernels
-    tune = None if (args.no_autotune or args.profile_only) else sim.autotune()
+    tune = None if (args.no_autotune or args.profile_only) else sim.autotune(vote=args.tune_vote)
+    if tune is not None:
+        args.vote_width = int(tune["vote_width"])
     force_error = None if args.profile_only else _step_error(sim, idx, O, np)
     clocks = ClockSampler(local) if rank == 0 else None
     if clocks:
@@ -428,6 +432,8 @@ def main():
     hbm_peak, peak_src = _peaks()
     geometry = {} if tune is None else {"force_threads": tune["force_threads"], "stack_cap": tune["stack_cap"],
                                         "build_phases": tune["build_phases"], "build_buckets": tune["build_buckets"]}
+    if tune is not None and args.tune_vote:
+        args.vote = int(tune["vote_width"])      # the other sims walk with the chosen width too
     ts = new_sim(stage_timing=True, **geometry)
     ts.step(2)
     tstream = torch.cuda.ExternalStream(ts.stream, device=dev)
@@ -557,7 +563,8 @@ def main():
             "stages": stages,
             "roofline": roofline,
             "autotune": None if tune is None else {k: tune[k] for k in (
-                "force_threads", "stack_cap", "build_phases", "build_buckets", "max_depth", "ms_force", "ms_force_before",
+                "force_threads", "stack_cap", "build_phases", "build_buckets", "vote_width", "max_depth", "ms_force",
+                "ms_force_before",
                 "ms_tree", "ms_tree_before")},
             "e2e": {"value": e2e_ms / div, "unit": "ms/step", "h2d_bytes_per_step": 36 * n,
                     "d2h_bytes_per_step": 36 * n, "wall_ms_per_step": wall_ms,
