@@ -54,6 +54,9 @@ struct nbh_sim {
     int4* buckets = nullptr;       // bucketed build: nbody records
     int* bwork = nullptr;          // bucketed build: 2 * nbody entries
     unsigned char* bstack = nullptr;   // bucketed build: per-warp task stacks
+    int* item_order = nullptr;     // force work items, longest walks first (nwarps entries)
+    int* item_cost = nullptr;      // visits of each item's last walk
+    int order_vote = 0;            // vote width the order is valid for (0: none)
     ThetaDev* model = nullptr;     // installed model (device)
     float* model_prm = nullptr;    // its FP32 parameters (device)
     float* probe_theta = nullptr;  // per-body theta of the last force probe (device)
@@ -113,7 +116,8 @@ int grow(nbh_sim* sim, T** ptr, size_t count, size_t* cap_unused = nullptr) {
 void free_buffers(nbh_sim* sim) {
     void* ptrs[] = {sim->probe_theta, sim->feat, sim->clevel, sim->probe, sim->loff, sim->kids4, sim->node4, sim->vel, sim->acc, sim->kpos, sim->kvel, sim->child, sim->count,
                     sim->start, sim->arrive, sim->parent, sim->sorted, sim->ubody, sim->ubox,
-                    sim->uradius, sim->chunks, sim->warps, sim->staging, sim->theta_body, sim->buckets, sim->bwork, sim->bstack};
+                    sim->uradius, sim->chunks, sim->warps, sim->staging, sim->theta_body, sim->buckets, sim->bwork, sim->bstack,
+                    sim->item_order, sim->item_cost};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     sim->kids4 = sim->node4 = sim->vel = sim->acc = sim->kpos = sim->kvel = nullptr;
@@ -130,6 +134,8 @@ void free_buffers(nbh_sim* sim) {
     sim->buckets = nullptr;
     sim->bwork = nullptr;
     sim->bstack = nullptr;
+    sim->item_order = sim->item_cost = nullptr;
+    sim->order_vote = 0;
     sim->cap_body = sim->cap_nodes = sim->cap_univ = sim->cap_chunks = sim->cap_warps = 0;
 }
 
@@ -160,6 +166,8 @@ StepParams step_params(const nbh_sim* sim) {
     p.buckets = sim->buckets;
     p.bwork = sim->bwork;
     p.bstack = sim->bstack;
+    p.item_order = sim->item_order;
+    p.item_cost = sim->item_cost;
     p.st = sim->st;
     p.ubody = sim->ubody;
     p.ubox = sim->ubox;
@@ -182,6 +190,19 @@ StepParams step_params(const nbh_sim* sim) {
     p.G = c.G;
     p.precise = c.precise;
     return p;
+}
+
+// Force work items of a vote width: 32-body items for widths 16 and 32, else 64 or 128.
+int nitems_for_vote(const nbh_sim* sim, int vote) {
+    return vote == 128 ? sim->nitems128 : (vote == 64 ? sim->nitems64 : sim->nwarps);
+}
+
+// The work-item order belongs to one item table (one vote width): start it over (index
+// order, no costs) when the width changes or new universes are loaded.
+void ensure_item_order(nbh_sim* sim) {
+    if (sim->order_vote == sim->cfg.vote_width) return;
+    launch_item_order_reset(nitems_for_vote(sim, sim->cfg.vote_width), sim->item_order, sim->item_cost, sim->stream);
+    sim->order_vote = sim->cfg.vote_width;
 }
 
 // Enqueue the six stages of one step (GPUBarnesHutNBodySimulation.java:258-263).
@@ -209,6 +230,8 @@ void enqueue_step(nbh_sim* sim, bool timed) {
     } else {
         launch_force(p, sim->cfg.vote_width, ref, sim->theta_active, sim->grid_force, sim->force_threads, s);
     }
+    // the next step hands out the longest walks first
+    launch_item_order(sim->item_cost, nitems_for_vote(sim, sim->cfg.vote_width), sim->item_order, s);
     if (timed) cudaEventRecord(sim->ev[5], s);
     launch_integrate(p, ref, sim->grid_int, s);
     if (timed) cudaEventRecord(sim->ev[6], s);
@@ -330,6 +353,8 @@ int alloc_for(nbh_sim* sim, int nbody, int nuniv, int nnodes, int nchunks, int n
     if ((e = grow(sim, &sim->buckets, (size_t)nbody))) return e;
     if ((e = grow(sim, &sim->bwork, 2 * (size_t)nbody))) return e;
     if ((e = grow(sim, &sim->bstack, bucket_stack_bytes(sim->sms)))) return e;
+    if ((e = grow(sim, &sim->item_order, (size_t)nwarps))) return e;
+    if ((e = grow(sim, &sim->item_cost, (size_t)nwarps))) return e;
     if ((e = grow(sim, &sim->probe_theta, (size_t)nbody))) return e;
     if ((e = grow(sim, &sim->feat, (size_t)nbody * kMlpIn))) return e;
     if ((e = grow(sim, &sim->start, (size_t)ncells))) return e;
@@ -648,6 +673,7 @@ int nbh_load_batch(nbh_sim* sim, int32_t nuniv, const int32_t* counts, const flo
     CK(cudaStreamSynchronize(s));
     drop_graph(sim);
     sim->theta_active = false;
+    sim->order_vote = 0;
     sim->loaded = true;
     sim->steps = 0;
     sim->last_err = NBH_OK;
@@ -664,6 +690,7 @@ int nbh_step_async(nbh_sim* sim, int32_t nsteps) {
     if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_step before nbh_load");
     if (nsteps < 0) return fail(sim, NBH_ERR_INVALID, "nsteps < 0");
     CK(cudaSetDevice(sim->device));
+    ensure_item_order(sim);
     const bool timed = sim->cfg.stage_timing != 0;
     for (int i = 0; i < nsteps; ++i) {
         if (timed || !sim->cfg.use_graph) {
@@ -1057,6 +1084,8 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
         StepParams q = step_params(sim);
         q.theta_body = nullptr;
         q.probe = sim->probe;           // results go to the scratch buffer, body state untouched
+        q.item_order = nullptr;         // index order (the step's order belongs to its own width)
+        q.item_cost = nullptr;
         q.stack_cap = g.second;
         const int grid = occ * sim->sms;
         float ms = 0.0f;
@@ -1279,6 +1308,8 @@ int nbh_force_probe(nbh_sim* sim, const float* theta_body, float* ax, float* ay,
     if ((e = rebuild_tree(sim, p))) return e;
     p.theta_body = sim->probe_theta;
     p.probe = sim->probe;
+    p.item_order = nullptr;             // a probe neither uses nor changes the step's work order
+    p.item_cost = nullptr;
     const int zero = 0;
     const unsigned long long z64 = 0;
     CK(cudaMemcpyAsync(&sim->st->force_next, &zero, sizeof(int), cudaMemcpyHostToDevice, s));

@@ -108,6 +108,8 @@ struct StepParams {
     int4* buckets;       // bucketed build: (slot, first entry, bodies, 0) per non-empty slot
     int* bwork;          // bucketed build: 2 * nbody entries (bodies of each bucket, ping-pong)
     void* bstack;        // bucketed build: per-warp task stacks of the large-bucket builder
+    const int* item_order; // force: work items in the order to hand them out (null: in index order)
+    int* item_cost;      // force: visits of each work item's walk, for the next step's order (may be null)
     int stack_cap;       // entries of each force group's shared-memory stack
     int theta_group;     // per-body theta: 1 = each vote group walks with its smallest angle
     int feat_gate;       // force launch gated on the learned-theta schedule: 0 none,

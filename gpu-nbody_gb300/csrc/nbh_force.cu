@@ -135,6 +135,7 @@ __global__ void __launch_bounds__(kForceThreadsMax) force_kernel(StepParams p) {
         if (lane == 0) item = atomicAdd(&p.st->force_next, 1);
         item = __shfl_sync(0xffffffffu, item, 0);
         if (item >= nitems) break;
+        if (p.item_order) item = p.item_order[item];   // costly items first (see item_order_kernel)
         const int2 wi = items[item];
         const int u = wi.y;
         const int uend = p.ubody[u + 1];
@@ -176,6 +177,7 @@ __global__ void __launch_bounds__(kForceThreadsMax) force_kernel(StepParams p) {
             }
         }
         long long ninter = 0;
+        int visits = 0;                                 // cost of this group's walk
         const int root = p.nnodes - u;
 
         if (gvalid) {
@@ -250,6 +252,7 @@ __global__ void __launch_bounds__(kForceThreadsMax) force_kernel(StepParams p) {
                     __syncwarp(gmask);     // every lane has read the stack before it is refilled
                 }
                 if (ok) ninter = pushed - opened;
+                visits = pushed;
             } else {
                 // Deep trees: per-level (cell, next child) walk (calculateforce.cl:112-172).
                 int depth = 0;
@@ -342,6 +345,13 @@ __global__ void __launch_bounds__(kForceThreadsMax) force_kernel(StepParams p) {
             }
             p.acc[b[k]] = make_float4(ax[k], ay[k], az[k], eb[k]);
         }
+        if (p.item_cost) {
+            // the item's cost: its group's visits (the deep walk counts accepted children);
+            // two half-warp groups (W = 16) add up
+            int c = visits > 0 ? visits : (int)min(ninter, (long long)0x7fffffff);
+            if (GL < 32) c += __shfl_down_sync(0xffffffffu, c, 16);
+            if (lane == 0) p.item_cost[item] = c;
+        }
         __syncwarp();
     }
 #pragma unroll
@@ -416,6 +426,62 @@ void launch_force(const StepParams& p, int vote, bool ref, bool feat, int grid, 
 
 // Resident blocks per SM of the fixed-angle variant at this geometry (the per-body
 // variants use as many registers or fewer per resident warp budget; their grid is the same).
+// Order of the force work items for the next step: longest walks first (longest-
+// processing-time first), so the few long walks -- bodies near a dense centre, or small
+// per-body angles -- start early instead of running alone at the end of the launch.  A
+// counting sort by floor(log2(cost)), descending; within a class the order is arbitrary.
+// One block; warp-aggregated shared-memory atomics.
+constexpr int kOrderThreads = 1024;
+__global__ void __launch_bounds__(kOrderThreads) item_order_kernel(const int* __restrict__ cost, int nitems,
+                                                                   int* order) {
+    __shared__ int cnt[32], off[32];
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    if (threadIdx.x < 32) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    for (int i0 = 0; i0 < nitems; i0 += blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        const bool v = i < nitems;
+        const int cls = v ? 31 - __clz(max(cost[i], 1)) : -1;
+        const unsigned grp = __match_any_sync(0xffffffffu, cls);
+        if (v && lane == __ffs(grp) - 1) atomicAdd(&cnt[cls], __popc(grp));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int sum = 0;
+        for (int c = 31; c >= 0; --c) {
+            off[c] = sum;
+            sum += cnt[c];
+        }
+    }
+    __syncthreads();
+    for (int i0 = 0; i0 < nitems; i0 += blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        const bool v = i < nitems;
+        const int cls = v ? 31 - __clz(max(cost[i], 1)) : -1;
+        const unsigned grp = __match_any_sync(0xffffffffu, cls);
+        const int leader = __ffs(grp) - 1;
+        int base = 0;
+        if (v && lane == leader) base = atomicAdd(&off[cls], __popc(grp));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (v) order[base + __popc(grp & lt)] = i;
+    }
+}
+
+__global__ void item_order_reset_kernel(int nitems, int* order, int* cost) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += gridDim.x * blockDim.x) {
+        order[i] = i;
+        cost[i] = 0;
+    }
+}
+
+void launch_item_order(const int* cost, int nitems, int* order, cudaStream_t s) {
+    if (nitems > 0) item_order_kernel<<<1, kOrderThreads, 0, s>>>(cost, nitems, order);
+}
+void launch_item_order_reset(int nitems, int* order, int* cost, cudaStream_t s) {
+    if (nitems > 0) item_order_reset_kernel<<<(nitems + 255) / 256, 256, 0, s>>>(nitems, order, cost);
+}
+
 int occupancy_force(int vote, bool ref, int threads, int cap, int* blocks_per_sm) {
     if (vote == 128)
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<128, false, false, false>,

@@ -16,6 +16,9 @@ void launch_summarize(const StepParams& p, bool ref, int grid, cudaStream_t s);
 void launch_sort(const StepParams& p, int grid, cudaStream_t s);
 void launch_force(const StepParams& p, int vote, bool ref, bool feat, int grid, int threads, cudaStream_t s);
 bool force_geometry_valid(int vote, int threads, int cap);
+// Work-item order of the force launches: longest walks first, from the last launch's costs.
+void launch_item_order(const int* cost, int nitems, int* order, cudaStream_t s);
+void launch_item_order_reset(int nitems, int* order, int* cost, cudaStream_t s);
 int force_fast_max_depth(int cap);   // deepest tree the stack of `cap` entries walks without the per-level walk
 void launch_integrate(const StepParams& p, bool ref, int grid, cudaStream_t s);
 
