@@ -10,9 +10,9 @@ force at the angle grid on sampled bodies and measures the error against the FP6
 sum.  Candidate models are fitted for several error budgets tau (fractions of the fixed
 theta = 0.5 p99 error) and loss quantiles, then validated on a third seed through the
 production step path (features and BF16 inference inside the step, the model evaluated
-every `--every` steps); of the candidates whose p99 error, averaged over one evaluation
-cycle of steps, does not exceed the fixed-theta p99 over the same steps, the fastest is
-kept.
+every `--every` steps), each with several floors of the predicted angle; of the candidates
+whose p99 error, averaged and at its worst over one evaluation cycle of steps, does not
+exceed the fixed-theta p99 over the same steps, the fastest is kept.
 """
 from __future__ import annotations
 
@@ -32,7 +32,7 @@ from nbh import learned as LR  # noqa: E402
 from nbh import universe as U  # noqa: E402
 
 
-def evaluate(arrs, model, theta=0.5, eps=0.05, dt=0.01, nsample=4096, warm=3, cycle=4, timed=8, seed=17,
+def evaluate(arrs, model, theta=0.5, eps=0.05, dt=0.01, nsample=4096, warm=3, cycle=4, timed=16, seed=17,
              device=0, every=None):
     """Fixed theta (plain) against the learned angle (if model) from the same initial
     state, through the production step: after `warm` steps, the relative force error
@@ -105,6 +105,9 @@ def study(n=1 << 20, seed=2024, grid=(0.4, 0.45, 0.5, 0.55, 0.6, 0.7, 0.8, 0.9, 
     return out
 
 
+FLOORS = (0.35, 0.4, 0.45, 0.5)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=1 << 20)
@@ -161,15 +164,21 @@ def main():
         Y = np.concatenate([np.tile(LR.theta_target(E, tau_frac * p99_plain), E.shape[0]) for E in Es])
         for q in (0.1, 0.2, 0.3):
             model = LR.train(X, Y, quantile=q, iters=args.iters)
-            model.update({"theta_min": 0.3, "theta_max": 1.0, "tau_frac": tau_frac, "tau": tau_frac * p99_plain,
+            model.update({"theta_max": 1.0, "tau_frac": tau_frac, "tau": tau_frac * p99_plain,
                           "every": args.every, "group": args.group})
-            r = evaluate(val, model)["learned"]
-            r.update({"tau_frac": tau_frac, "quantile": q, "loss": model["loss"],
-                      "interaction_gain": base["interactions"] / r["interactions"],
-                      "speedup": base["ms_per_step"] / r["ms_per_step"], "p99_ratio": r["p99"] / base["p99"]})
-            print(json.dumps(r), flush=True)
-            if r["p99"] <= base["p99"] and (best is None or r["ms_per_step"] < best[1]["ms_per_step"]):
-                best = (model, r)
+            # the angle's floor is an inference-time clamp: a floor too low lets a few groups
+            # walk at a very small angle, and their long walks become the launch's tail
+            for floor in FLOORS:
+                model["theta_min"] = floor
+                r = evaluate(val, model)["learned"]
+                r.update({"tau_frac": tau_frac, "quantile": q, "theta_min": floor, "loss": model["loss"],
+                          "interaction_gain": base["interactions"] / r["interactions"],
+                          "speedup": base["ms_per_step"] / r["ms_per_step"], "p99_ratio": r["p99"] / base["p99"],
+                          "p99_max_ratio": r["p99_max"] / base["p99_max"]})
+                print(json.dumps(r), flush=True)
+                if (r["p99"] <= base["p99"] and r["p99_max"] <= base["p99_max"]
+                        and (best is None or r["ms_per_step"] < best[1]["ms_per_step"])):
+                    best = (dict(model), r)
     if best is None:
         raise SystemExit("no candidate met the fixed-theta p99 error")
     model, r = best
