@@ -10,7 +10,7 @@ force at the angle grid on sampled bodies and measures the error against the FP6
 sum.  Candidate models are fitted for several error budgets tau (fractions of the fixed
 theta = 0.5 p99 error) and loss quantiles, then validated on a third seed through the
 production step path (features and BF16 inference inside the step, the model evaluated
-every `--every` steps), each with several floors of the predicted angle; of the candidates
+every 4 or 8 steps), each with several floors of the predicted angle; of the candidates
 whose p99 error, averaged and at its worst over one evaluation cycle of steps, does not
 exceed the fixed-theta p99 over the same steps, the fastest is kept.
 """
@@ -106,6 +106,7 @@ def study(n=1 << 20, seed=2024, grid=(0.4, 0.45, 0.5, 0.55, 0.6, 0.7, 0.8, 0.9, 
 
 
 FLOORS = (0.35, 0.4, 0.45, 0.5)
+EVERY = (4, 8)            # steps between evaluations of the model
 
 
 def main():
@@ -114,7 +115,6 @@ def main():
     ap.add_argument("--samples", type=int, default=6144)
     ap.add_argument("--out", default=LR.default_model_path())
     ap.add_argument("--iters", type=int, default=1500)
-    ap.add_argument("--every", type=int, default=4, help="steps between model evaluations")
     ap.add_argument("--group", type=int, default=0, help="1: each vote group walks with its smallest angle")
     ap.add_argument("--study", action="store_true", help="measure the ceiling of a per-body angle and exit")
     args = ap.parse_args()
@@ -160,18 +160,19 @@ def main():
     print("validation plain:", base, flush=True)
     best = None
     X = np.concatenate([F.reshape(-1, 12) for F in Fs])
-    for tau_frac in (0.4, 0.5, 0.6, 0.7):
+    for tau_frac in (0.4, 0.5, 0.6, 0.7, 0.8):
         Y = np.concatenate([np.tile(LR.theta_target(E, tau_frac * p99_plain), E.shape[0]) for E in Es])
         for q in (0.1, 0.2, 0.3):
             model = LR.train(X, Y, quantile=q, iters=args.iters)
             model.update({"theta_max": 1.0, "tau_frac": tau_frac, "tau": tau_frac * p99_plain,
-                          "every": args.every, "group": args.group})
+                          "group": args.group})
             # the angle's floor is an inference-time clamp: a floor too low lets a few groups
             # walk at a very small angle, and their long walks become the launch's tail
-            for floor in FLOORS:
+            for floor, every in [(f, e) for f in FLOORS for e in EVERY]:
                 model["theta_min"] = floor
+                model["every"] = every
                 r = evaluate(val, model)["learned"]
-                r.update({"tau_frac": tau_frac, "quantile": q, "theta_min": floor, "loss": model["loss"],
+                r.update({"tau_frac": tau_frac, "quantile": q, "theta_min": floor, "every": every, "loss": model["loss"],
                           "interaction_gain": base["interactions"] / r["interactions"],
                           "speedup": base["ms_per_step"] / r["ms_per_step"], "p99_ratio": r["p99"] / base["p99"],
                           "p99_max_ratio": r["p99_max"] / base["p99_max"]})
