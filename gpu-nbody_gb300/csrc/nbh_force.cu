@@ -56,7 +56,7 @@ __device__ __forceinline__ void interact(const float4 q, const float dx, const f
     ax = madd<REF>(dx, f, ax);
     ay = madd<REF>(dy, f, ay);
     az = madd<REF>(dz, f, az);
-    if constexpr (FEAT) eb = __fadd_rn(eb, __fmul_rn(__fmul_rn(f, rd), s2));
+    if constexpr (FEAT) eb = __fmaf_rn(__fmul_rn(f, rd), s2, eb);
 }
 
 template <bool REF>
@@ -234,7 +234,9 @@ __global__ void __launch_bounds__(kForceThreadsMax) force_kernel(StepParams p) {
                             dy[k] = __fsub_rn(q.y, pb[k].y);
                             dz[k] = __fsub_rn(q.z, pb[k].z);
                             d2[k] = dist2<REF>(dx[k], dy[k], dz[k], eps2);
-                            const float dq = kStoreDq ? sl : __fadd_rn(__fmul_rn(t0[k], sl), eps2);
+                            // t0 * 4^-level is exact (a power of two), so one fused op gives the
+                            // same threshold as the rounded product and sum
+                            const float dq = kStoreDq ? sl : __fmaf_rn(t0[k], sl, eps2);
                             pass = pass && d2[k] >= dq;
                         }
                         if (__all_sync(gmask, pass)) {
