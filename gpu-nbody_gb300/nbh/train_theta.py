@@ -106,7 +106,7 @@ def study(n=1 << 20, seed=2024, grid=(0.4, 0.45, 0.5, 0.55, 0.6, 0.7, 0.8, 0.9, 
 
 
 FLOORS = (0.35, 0.4, 0.45, 0.5)
-EVERY = (4, 8)            # steps between evaluations of the model
+EVERY = (4, 8, 16)        # steps between evaluations of the model
 
 
 def main():
