@@ -484,17 +484,21 @@ def main():
     e2e_ev = []
     t_wall = time.perf_counter()
     for _ in range(e2e_steps):
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record(stream)
         sim.write(*[hin[k] for k in keys])
+        ev[1].record(stream)
         sim.step(1)
+        ev[2].record(stream)
         sim.read_into(*[hout[k] for k in keys])
-        e1.record(stream)
-        e2e_ev.append((e0, e1))
+        ev[3].record(stream)
+        e2e_ev.append(ev)
     torch.cuda.synchronize(dev)
     wall_ms = 1e3 * (time.perf_counter() - t_wall) / e2e_steps
-    e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_ev) / e2e_steps
+    e2e_ms = sum(ev[0].elapsed_time(ev[3]) for ev in e2e_ev) / e2e_steps
+    # device time of each part (the gaps between the calls' synchronisations included)
+    e2e_parts = {name: sum(ev[i].elapsed_time(ev[i + 1]) for ev in e2e_ev) / e2e_steps
+                 for i, name in enumerate(("write_ms", "step_ms", "read_ms"))}
     if dist:
         t = torch.tensor([e2e_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -567,7 +571,7 @@ def main():
                 "ms_force_before",
                 "ms_tree", "ms_tree_before")},
             "e2e": {"value": e2e_ms / div, "unit": "ms/step", "h2d_bytes_per_step": 36 * n,
-                    "d2h_bytes_per_step": 36 * n, "wall_ms_per_step": wall_ms,
+                    "d2h_bytes_per_step": 36 * n, "wall_ms_per_step": wall_ms, "parts": e2e_parts,
                     "path": "nbh_write (pinned host) -> nbh_step -> nbh_read (pinned host)"},
             "gpu_launches": graph_launches(**({"build_phases": tune["build_phases"], "build_buckets": tune["build_buckets"]}
                                               if tune else {})) * args.steps,

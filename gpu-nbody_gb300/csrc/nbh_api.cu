@@ -1134,8 +1134,11 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
     CK(cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (sim->h_state->status != NBH_OK) return fail(sim, sim->h_state->status, "nbh_autotune: a timed launch failed");
-    // the state word as it was (the tree is rebuilt by the next step in any case)
+    // the state word as it was (the tree is rebuilt by the next step in any case), except
+    // the record of the pool slots the timed builds wrote, which the next reset must cover
+    const int pool_low = std::min(sim->h_state->pool_low, sim->h_state->bottom);
     *sim->h_state = saved;
+    sim->h_state->pool_low = std::min(saved.pool_low, pool_low);
     CK(cudaMemcpyAsync(sim->st, sim->h_state, sizeof(DevState), cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
     sim->force_threads = best_t;

@@ -58,7 +58,7 @@ struct DevState {
     int bucket_fill;     // bucketed build: entries handed out in the bucket work list
     int nbuckets;        // bucketed build: non-empty slots of the sampled tree
     int bucket_next;     // bucketed build: work counter of the subtree builders
-    int pad1;
+    int pool_low;        // lowest cell whose slots a build may have written since the last reset
     unsigned long long pad2;
     // Build contention meters, spread over kDiagSlots addresses so that counting does not
     // itself serialise: descents that found their slot locked, and lost lock races.

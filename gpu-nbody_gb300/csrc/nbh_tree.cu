@@ -26,6 +26,20 @@ __global__ void __launch_bounds__(256) bbox_kernel(StepParams p) {
     __shared__ float red[6][8];
     __shared__ int last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    {
+        // Empty the slots of every cell a build may have written since the last reset (the
+        // whole pool after a load, when bottom is 0), so that the insertion of this step
+        // finds in any slot only kNull or a value written during this step -- see
+        // build_kernel for why that matters.  Every block reads the bounds before the last
+        // block moves them (below, after all blocks have taken their ticket).
+        const int lo = max(p.nbody + 1, min(p.st->pool_low, p.st->bottom));
+        const int hi = p.nnodes - p.nuniv;     // the roots above are reset below
+        int4* const c4 = reinterpret_cast<int4*>(p.child);
+        const int4 empty = make_int4(kNull, kNull, kNull, kNull);
+        for (long long i = 2LL * lo + (long long)blockIdx.x * blockDim.x + threadIdx.x; i <= 2LL * hi + 1;
+             i += (long long)gridDim.x * blockDim.x)
+            c4[i - 2LL * p.nbody] = empty;
+    }
     for (int ci = blockIdx.x; ci < p.nchunks;) {
         // fold this block's consecutive chunks of one universe, then publish once
         const int u = p.chunks[ci].x;
@@ -114,6 +128,7 @@ __global__ void __launch_bounds__(256) bbox_kernel(StepParams p) {
     if (threadIdx.x == 0) {
         DevState* st = p.st;
         st->bottom = p.nnodes - p.nuniv + 1;
+        st->pool_low = st->bottom;          // nothing below the roots is written now
         st->bbox_ticket = 0;
         st->step += 1;
         st->force_next = 0;
@@ -185,11 +200,16 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p, BuildPhase pha
             float cx = rc.x, cy = rc.y, cz = rc.z;
             int path = octant(cx, cy, cz, bp.x, bp.y, bp.z);
             int* slot = cell_child(p, node) + path;
-            // Slots are read through L1.  A slot that holds a cell index keeps it for the
-            // rest of the build, and each cell's slots are one 32-byte sector first read
-            // after the cell was published, so a cell index read from L1 is always right;
-            // any other value is only acted on through the CAS below, which fails if it is
-            // stale and returns the current value.  This keeps the descents off the L2
+            // Slots are read through L1 and without acquire, so a read may return an older
+            // value of the slot.  That is safe because of what a slot can have held: the
+            // bbox stage empties every pool slot a build wrote (kNull), and during the
+            // build a slot only goes kNull -> body -> cell, with kLock in between; a cell
+            // index, once stored, stays.  A cell index read is therefore always the
+            // current one, and any other value is only acted on through the CAS below,
+            // which fails if it is stale and returns the current value.  The reset keeps
+            // this true whatever the L1 holds: a sector of a newly taken cell cached before
+            // the cell was initialised can only show kNull, never a child index left by
+            // the previous step's tree.  Reading through L1 keeps the descents off the L2
             // lines of the top cells.
             int ch = __ldca(slot);
             for (;;) {
@@ -714,18 +734,26 @@ __global__ void __launch_bounds__(32 * kBucketWarps) bucket_build_kernel(StepPar
 // Link: parent[] of every node from the finished tree (one pass over the cells), for the
 // bottom-up summarize, the sort's walk-up and the learned angle's features (a body's leaf
 // cell).  Keeping it out of the build means an insertion publishes nothing but a slot value.
+// It also tags each cell's count with its number of cell children k, as -1 - k: summarize
+// decides from this tag, which nothing changes until the cell is summed, and never from the
+// cell's slots, which the cell's summation rewrites (compaction) while other threads run.
 __global__ void __launch_bounds__(256) link_kernel(StepParams p) {
     if (load_status(p.st)) return;
     const int bottom = p.st->bottom;
+    const int nbody = p.nbody;
     const int stride = gridDim.x * blockDim.x;
     for (int c = bottom + (int)(blockIdx.x * blockDim.x + threadIdx.x); c <= p.nnodes; c += stride) {
         const int* ch8 = cell_child(p, c);
         const int4 s0 = reinterpret_cast<const int4*>(ch8)[0];
         const int4 s1 = reinterpret_cast<const int4*>(ch8)[1];
         const int sl[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+        int kc = 0;
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
+        for (int j = 0; j < 8; ++j) {
             if (sl[j] >= 0) p.parent[sl[j]] = c;
+            kc += sl[j] >= nbody;
+        }
+        p.count[c - nbody] = -1 - kc;
     }
 }
 
@@ -760,21 +788,17 @@ __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
     const int stride = gridDim.x * blockDim.x;
     const int bottom = ld_relaxed(&p.st->bottom);
     for (int c0 = bottom + (int)(blockIdx.x * blockDim.x + threadIdx.x); c0 <= p.nnodes; c0 += stride) {
+        // link's tag -1 - (cell children): only a cell without cell children starts here; the
+        // others are summed by their last cell child (tag < -1), perhaps already (tag >= 0)
+        if (p.count[c0 - nbody] != -1) continue;
         int c = c0;
-        bool start = true;
-        while (c >= 0) {
+        for (;;) {
+            // Every cell child of c has been summed and no other thread touches c now, so
+            // its slots are stable until the compaction below.
             int* ch8 = cell_child(p, c);
             const int4 s0 = reinterpret_cast<const int4*>(ch8)[0];
             const int4 s1 = reinterpret_cast<const int4*>(ch8)[1];
             const int sl[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
-            int kc = 0;                               // cell children
-#pragma unroll
-            for (int j = 0; j < 8; ++j) kc += sl[j] >= nbody;
-            if (start) {
-                if (kc > 0) break;                    // summed later by its last cell child
-            } else if (arrive_acq_rel(p.arrive + (c - nbody)) != kc - 1) {
-                break;                                // another cell child is still to come
-            }
             int used = 0, cnt = 0;
             float cm = 0.0f, sx = 0.0f, sy = 0.0f, sz = 0.0f;
             double dm = 0.0, dx = 0.0, dy = 0.0, dz = 0.0;
@@ -821,12 +845,16 @@ __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
                 p.node4[c] = make_float4(__fmul_rn(sx, inv), __fmul_rn(sy, inv), __fmul_rn(sz, inv), cm);
             }
             const int pc = p.parent[c];
-            if (pc >= 0 && pc <= c) {   // parents always have higher indices
+            if (pc < 0) break;          // a root
+            if (pc <= c) {              // parents always have higher indices
                 raise_error(p.st, NBH_ERR_STATE);
                 break;
             }
+            // pc is summed only after all its cell children arrive, this one included, so
+            // its tag still holds link's value
+            const int kc = -1 - __ldcg(p.count + (pc - nbody));
+            if (arrive_acq_rel(p.arrive + (pc - nbody)) != kc - 1) break;   // another child is to come
             c = pc;
-            start = false;
         }
     }
 }
