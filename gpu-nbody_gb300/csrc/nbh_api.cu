@@ -715,11 +715,10 @@ int nbh_synchronize(nbh_sim* sim) {
     return NBH_OK;
 }
 
-int nbh_step(nbh_sim* sim, int32_t nsteps) {
-    int e = nbh_step_async(sim, nsteps);
-    if (e) return e;
-    CK(cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, sim->stream));
-    CK(cudaStreamSynchronize(sim->stream));
+namespace {
+
+// After the stream has drained: the stage times of a timed step and the device status.
+int finish_steps(nbh_sim* sim, int32_t nsteps) {
     if (sim->cfg.stage_timing && nsteps > 0) {
         for (int k = 0; k < 6; ++k) cudaEventElapsedTime(&sim->stage_ms[k], sim->ev[k], sim->ev[k + 1]);
         cudaEventElapsedTime(&sim->stage_ms[6], sim->ev[0], sim->ev[6]);
@@ -735,19 +734,15 @@ int nbh_step(nbh_sim* sim, int32_t nsteps) {
     return NBH_OK;
 }
 
-int nbh_read(nbh_sim* sim, float* x, float* y, float* z, float* vx, float* vy, float* vz, float* ax, float* ay,
-             float* az) {
-    if (!sim) return NBH_ERR_INVALID;
-    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_read before nbh_load");
-    CK(cudaSetDevice(sim->device));
+// nbh_read without the wait: mapped pinned arrays are written in place by one kernel, other
+// arrays through the staging buffer and one copy each.
+int enqueue_read(nbh_sim* sim, float* const dst[9]) {
     const int n = sim->nbody;
     cudaStream_t s = sim->stream;
-    float* dst[9] = {x, y, z, vx, vy, vz, ax, ay, az};
     HostArrays h;
-    if (mapped_host_views(dst, n, &h)) {       // pinned caller arrays: written in place
+    if (mapped_host_views(dst, n, &h)) {
         launch_unpack_host(n, h, sim->node4, sim->vel, sim->acc, std::max(1, (n + 255) / 256), s);
         CK(cudaGetLastError());
-        CK(cudaStreamSynchronize(s));
         return NBH_OK;
     }
     launch_unpack(n, sim->staging, sim->node4, sim->vel, sim->acc, std::max(1, std::min((n + 255) / 256, 4 * sim->sms)),
@@ -756,7 +751,56 @@ int nbh_read(nbh_sim* sim, float* x, float* y, float* z, float* vx, float* vy, f
     for (int k = 0; k < 9; ++k)
         if (dst[k])
             CK(cudaMemcpyAsync(dst[k], sim->staging + (size_t)k * n, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    return NBH_OK;
+}
+
+// nbh_write without the wait (same checks and the same two paths as enqueue_read).
+int enqueue_write(nbh_sim* sim, const float* const in[9]) {
+    if ((in[0] || in[1] || in[2]) && !(in[0] && in[1] && in[2]))
+        return fail(sim, NBH_ERR_INVALID, "positions need x, y and z");
+    if ((in[3] || in[4] || in[5]) && !(in[3] && in[4] && in[5]))
+        return fail(sim, NBH_ERR_INVALID, "velocities need vx, vy and vz");
+    if ((in[6] || in[7] || in[8]) && !(in[6] && in[7] && in[8]))
+        return fail(sim, NBH_ERR_INVALID, "accelerations need ax, ay and az");
+    const int n = sim->nbody;
+    const float* src[10];
+    for (int k = 0; k < 9; ++k) src[k] = in[k];
+    src[9] = nullptr;
+    const int mask = (in[0] ? 1 : 0) | (in[3] ? 2 : 0) | (in[6] ? 4 : 0);
+    if (!mask) return NBH_OK;
+    HostArrays h;
+    if (mapped_host_views(src, n, &h)) {
+        launch_pack_host(n, h, mask, sim->node4, sim->vel, sim->acc, std::max(1, (n + 255) / 256), sim->stream);
+        CK(cudaGetLastError());
+        return NBH_OK;
+    }
+    int e;
+    if ((e = upload_soa(sim, n, src))) return e;
+    launch_pack(n, sim->staging, mask, sim->node4, sim->vel, sim->acc, std::max(1, std::min((n + 255) / 256, 4 * sim->sms)),
+                sim->stream);
+    CK(cudaGetLastError());
+    return NBH_OK;
+}
+
+}  // namespace
+
+int nbh_step(nbh_sim* sim, int32_t nsteps) {
+    int e = nbh_step_async(sim, nsteps);
+    if (e) return e;
+    CK(cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, sim->stream));
+    CK(cudaStreamSynchronize(sim->stream));
+    return finish_steps(sim, nsteps);
+}
+
+int nbh_read(nbh_sim* sim, float* x, float* y, float* z, float* vx, float* vy, float* vz, float* ax, float* ay,
+             float* az) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_read before nbh_load");
+    CK(cudaSetDevice(sim->device));
+    float* const dst[9] = {x, y, z, vx, vy, vz, ax, ay, az};
+    int e = enqueue_read(sim, dst);
+    if (e) return e;
+    CK(cudaStreamSynchronize(sim->stream));
     return NBH_OK;
 }
 
@@ -764,28 +808,32 @@ int nbh_write(nbh_sim* sim, const float* x, const float* y, const float* z, cons
               const float* vz, const float* ax, const float* ay, const float* az) {
     if (!sim) return NBH_ERR_INVALID;
     if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_write before nbh_load");
-    if ((x || y || z) && !(x && y && z)) return fail(sim, NBH_ERR_INVALID, "positions need x, y and z");
-    if ((vx || vy || vz) && !(vx && vy && vz)) return fail(sim, NBH_ERR_INVALID, "velocities need vx, vy and vz");
-    if ((ax || ay || az) && !(ax && ay && az)) return fail(sim, NBH_ERR_INVALID, "accelerations need ax, ay and az");
     CK(cudaSetDevice(sim->device));
-    const int n = sim->nbody;
-    const float* src[10] = {x, y, z, vx, vy, vz, ax, ay, az, nullptr};
-    const int mask = (x ? 1 : 0) | (vx ? 2 : 0) | (ax ? 4 : 0);
-    HostArrays h;
-    if (mask && mapped_host_views(src, n, &h)) {   // pinned caller arrays: read in place
-        launch_pack_host(n, h, mask, sim->node4, sim->vel, sim->acc, std::max(1, (n + 255) / 256), sim->stream);
-        CK(cudaGetLastError());
-        CK(cudaStreamSynchronize(sim->stream));
-        return NBH_OK;
-    }
-    int e;
-    if ((e = upload_soa(sim, n, src))) return e;
-    if (mask)
-        launch_pack(n, sim->staging, mask, sim->node4, sim->vel, sim->acc,
-                    std::max(1, std::min((n + 255) / 256, 4 * sim->sms)), sim->stream);
-    CK(cudaGetLastError());
+    const float* const in[9] = {x, y, z, vx, vy, vz, ax, ay, az};
+    int e = enqueue_write(sim, in);
+    if (e) return e;
     CK(cudaStreamSynchronize(sim->stream));
     return NBH_OK;
+}
+
+int nbh_step_io(nbh_sim* sim, int32_t nsteps, const nbh_host_state* in, const nbh_host_state* out) {
+    if (!sim) return NBH_ERR_INVALID;
+    if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_step_io before nbh_load");
+    if (nsteps < 0) return fail(sim, NBH_ERR_INVALID, "nsteps < 0");
+    CK(cudaSetDevice(sim->device));
+    int e;
+    if (in) {
+        const float* const src[9] = {in->x, in->y, in->z, in->vx, in->vy, in->vz, in->ax, in->ay, in->az};
+        if ((e = enqueue_write(sim, src))) return e;
+    }
+    if ((e = nbh_step_async(sim, nsteps))) return e;
+    CK(cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, sim->stream));
+    if (out) {
+        float* const dst[9] = {out->x, out->y, out->z, out->vx, out->vy, out->vz, out->ax, out->ay, out->az};
+        if ((e = enqueue_read(sim, dst))) return e;
+    }
+    CK(cudaStreamSynchronize(sim->stream));
+    return finish_steps(sim, nsteps);
 }
 
 int nbh_get_stats(nbh_sim* sim, nbh_stats* out) {

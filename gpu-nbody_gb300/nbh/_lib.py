@@ -86,6 +86,10 @@ class NbhTune(C.Structure):
     ]
 
 
+class NbhHostState(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az")]
+
+
 _P = C.c_void_p
 _F = C.POINTER(C.c_float)
 _I = C.POINTER(C.c_int32)
@@ -103,6 +107,7 @@ SIGNATURES = {
     "nbh_synchronize": (C.c_int, [_P]),
     "nbh_read": (C.c_int, [_P] + [_P] * 9),
     "nbh_write": (C.c_int, [_P] + [_P] * 9),
+    "nbh_step_io": (C.c_int, [_P, C.c_int32, C.POINTER(NbhHostState), C.POINTER(NbhHostState)]),
     "nbh_get_stats": (C.c_int, [_P, C.POINTER(NbhStats)]),
     "nbh_get_number_of_bodies": (C.c_int32, [_P]),
     "nbh_export_float4": (C.c_int, [_P, _P, _P]),

@@ -127,6 +127,34 @@ class Simulation:
         arr = [_f32(a) for a in (x, y, z, vx, vy, vz, ax, ay, az)]
         self._check(self._L.nbh_write(self._h, *[_ptr(a) for a in arr]))
 
+    def step_io(self, nsteps=1, write=None, read=None):
+        """nbh_step_io: `write` (dict of host arrays by component name, written before the
+        steps) and `read` (dict of float32 arrays filled after them), one wait in all."""
+        def state(d, conv):
+            if d is None:
+                return None, None
+            arrs = {k: conv(v) for k, v in d.items()}
+            bad = set(arrs) - {k for k, _ in L.NbhHostState._fields_}
+            if bad:
+                raise ValueError("unknown components %s" % sorted(bad))
+            return L.NbhHostState(**{k: _ptr(a) for k, a in arrs.items()}), arrs
+
+        def in_array(a):
+            a = _f32(a)
+            if a.size != self.n:
+                raise ValueError("write arrays must have n elements")
+            return a
+
+        def out_array(a):
+            if a.dtype != np.float32 or not a.flags.c_contiguous or a.size != self.n:
+                raise ValueError("read arrays must be contiguous float32 of n elements")
+            return a
+        sin, keep_in = state(write, in_array)
+        sout, keep_out = state(read, out_array)
+        self._check(self._L.nbh_step_io(self._h, int(nsteps), C.byref(sin) if sin else None,
+                                        C.byref(sout) if sout else None))
+        del keep_in, keep_out
+
     def stats(self) -> dict:
         s = L.NbhStats()
         self._check(self._L.nbh_get_stats(self._h, C.byref(s)))

@@ -162,6 +162,18 @@ int nbh_write(nbh_sim* sim, const float* x, const float* y, const float* z,
               const float* vx, const float* vy, const float* vz,
               const float* ax, const float* ay, const float* az);
 
+/* The nine host arrays of nbh_write / nbh_read (n floats each; NULL: not copied). */
+typedef struct nbh_host_state {
+    float *x, *y, *z, *vx, *vy, *vz, *ax, *ay, *az;
+} nbh_host_state;
+
+/* For a host that owns the state between steps: writes `in` like nbh_write (in may be
+ * NULL), runs nsteps steps like nbh_step, reads the state into `out` like nbh_read (out
+ * may be NULL), and waits once at the end instead of after each of the three calls.
+ * Pinned (mapped) arrays are read and written in place by the packing kernels.  Returns
+ * what nbh_step would. */
+int nbh_step_io(nbh_sim* sim, int32_t nsteps, const nbh_host_state* in, const nbh_host_state* out);
+
 int nbh_get_stats(nbh_sim* sim, nbh_stats* out);
 int32_t nbh_get_number_of_bodies(nbh_sim* sim);   /* getNumberOfBodies(), :376-379 */
 

@@ -48,7 +48,8 @@ def test_struct_layouts_match_the_c_compiler(tmp_path):
     import subprocess
     if shutil.which("gcc") is None:
         pytest.skip("gcc not available")
-    structs = {"nbh_config": L.NbhConfig, "nbh_stats": L.NbhStats, "nbh_diag": L.NbhDiag, "nbh_tune": L.NbhTune}
+    structs = {"nbh_config": L.NbhConfig, "nbh_stats": L.NbhStats, "nbh_diag": L.NbhDiag, "nbh_tune": L.NbhTune,
+               "nbh_host_state": L.NbhHostState}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "nbh.h"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))

@@ -351,6 +351,63 @@ def test_pinned_host_arrays_match_the_staged_path():
         np.testing.assert_array_equal(res[True][k], res[False][k])
 
 
+def test_step_io_equals_write_step_read():
+    """nbh_step_io (write, steps, read, one wait) gives exactly what nbh_write + nbh_step +
+    nbh_read give, with pinned and with pageable arrays, and with only one of its two parts;
+    a write of positions only keeps velocities and accelerations."""
+    torch = pytest.importorskip("torch")
+    n = 30000
+    arrs = plummer(n, seed=92)
+    keys = ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az")
+
+    def fresh():
+        g = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+        g.load(*arrs)
+        g.step(2)
+        return g
+    g = fresh()
+    st = g.read()
+    hin = {k: st[k] * np.float32(1.0 + 1e-3) for k in keys}
+    g.write(*[hin[k] for k in keys])
+    g.step(3)
+    want = g.read()
+    g.close()
+    for pinned in (False, True):
+        if pinned:
+            src = {k: torch.empty(n, dtype=torch.float32, pin_memory=True).numpy() for k in keys}
+            out = {k: torch.empty(n, dtype=torch.float32, pin_memory=True).numpy() for k in keys}
+        else:
+            src = {k: np.empty(n, np.float32) for k in keys}
+            out = {k: np.empty(n, np.float32) for k in keys}
+        for k in keys:
+            src[k][:] = hin[k]
+        g = fresh()
+        g.step_io(3, write=src, read=out)
+        for k in keys:
+            np.testing.assert_array_equal(out[k], want[k], err_msg="%s pinned=%s" % (k, pinned))
+        g.close()
+    # write only, then read only; positions only leave the rest as they were
+    g = fresh()
+    g.step_io(0, write={k: hin[k] for k in keys})
+    g.step_io(3)
+    part = {k: np.empty(n, np.float32) for k in ("x", "vz")}
+    g.step_io(0, read=part)
+    np.testing.assert_array_equal(part["x"], want["x"])
+    np.testing.assert_array_equal(part["vz"], want["vz"])
+    before = g.read()
+    g.step_io(0, write={"x": hin["x"], "y": hin["y"], "z": hin["z"]})
+    after = g.read()
+    np.testing.assert_array_equal(after["x"], hin["x"])
+    for k in ("vx", "vy", "vz", "ax", "ay", "az"):
+        np.testing.assert_array_equal(after[k], before[k])
+    import nbh
+    from nbh import _lib as L
+    with pytest.raises(nbh.NbhError) as ei:
+        g.step_io(1, write={"x": hin["x"]})           # positions need x, y and z
+    assert ei.value.code == L.NBH_ERR_INVALID
+    g.close()
+
+
 def test_massless_tracers_match_oracle():
     """A quarter of the bodies carry no mass (tracers).  Cells holding only tracers have no
     defined centre of mass (0/0, as in the reference's summarize), never pass the opening
