@@ -463,6 +463,7 @@ constexpr int kBucketWarps = 4;
 constexpr int kBucketStack = 232;
 constexpr int kSmallStack = 48;
 constexpr int kBucketBlocksPerSm = 9;
+constexpr int kBucketChunk = 4;      // buckets a warp takes per work-counter atomic
 
 // Stack position of each child cell among the nc cells pushed now: the largest deepest.
 __device__ __forceinline__ int deeper_rank(int mycnt, int lane) {
@@ -476,13 +477,17 @@ __device__ __forceinline__ int deeper_rank(int mycnt, int lane) {
 }
 
 // The subtree of the m <= 32 bodies src[lo, lo + m) below a cell of level `level` with the
-// given centre and half-width.  cell >= 0: that cell exists already (its slots are written
-// here); cell < 0: it is taken from the pool with the rest.  Returns the subtree's root cell
-// (or -1 after raising an error).  Whole-warp call.  Lanes with a body are grouped by octant
-// (match_any); each group's lowest lane writes its octant's slot -- its own body when alone,
-// else a new cell -- and lanes 0..7 write the empty octants.
-__device__ int build_small(const StepParams& p, const int* __restrict__ src, int lo, int m, int cell, int level,
-                           float cx, float cy, float cz, float r, SmallTask* st, int& local_max) {
+// given centre and half-width, in one of two passes over the same traversal.  Counting
+// (build = false) returns the number of new cells the subtree takes and writes nothing.
+// Building (build = true) takes them as base - 1, base - 2, ... (parents first, so every
+// parent index is above its children's) and returns the subtree's root: `cell` when it
+// exists already (its slots are written here), else base - 1.  Returns -1 after raising
+// an error.  Whole-warp call.  Lanes with a body are grouped by octant (match_any); each
+// group's lowest lane writes its octant's slot -- its own body when alone, else a new cell
+// -- and lanes 0..7 write the empty octants.
+__device__ int small_subtree(const StepParams& p, const int* __restrict__ src, int lo, int m, int cell, int level,
+                             float cx, float cy, float cz, float r, SmallTask* st, int& local_max, bool build,
+                             int base) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int nbody = p.nbody;
@@ -493,75 +498,79 @@ __device__ int build_small(const StepParams& p, const int* __restrict__ src, int
         q = p.node4[b];
     }
     const unsigned all = m >= 32 ? 0xffffffffu : ((1u << m) - 1u);
-    int base = 0, next = 0;
-    for (int pass = 0; pass < 2; ++pass) {           // 0: count the cells, 1: build
-        int made = 0;
-        if (pass == 1 && next > 0) {
-            if (lane == 0) base = atomicSub(&p.st->bottom, next);
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (base - next <= nbody) {
-                raise_error(p.st, NBH_ERR_POOL);
-                return -1;
-            }
-        }
-        int root = cell;
-        if (cell < 0) root = pass == 1 ? base - 1 - made++ : (made++, 0);
-        if (lane == 0) st[0] = SmallTask{all, root, level, cx, cy, cz, r};
-        int top = 1;
+    int made = 0;
+    int root = cell;
+    if (cell < 0) root = build ? base - 1 - made++ : (made++, 0);
+    if (lane == 0) st[0] = SmallTask{all, root, level, cx, cy, cz, r};
+    int top = 1;
+    __syncwarp();
+    while (top > 0) {
+        const SmallTask t = st[--top];
         __syncwarp();
-        while (top > 0) {
-            const SmallTask t = st[--top];
-            __syncwarp();
-            const bool member = (t.mask >> lane) & 1u;
-            const int o = member ? octant(t.cx, t.cy, t.cz, q.x, q.y, q.z) : -1;
-            const unsigned grp = __match_any_sync(0xffffffffu, o);
-            const bool leader = member && (__ffs(grp) - 1) == lane;
-            const int cnt = __popc(grp);
-            const unsigned balc = __ballot_sync(0xffffffffu, leader && cnt >= 2);
-            const int nc = __popc(balc);
-            if (nc > 0 && (t.level + 2 > kMaxDepth || top + nc > kSmallStack)) {   // coincident bodies
-                raise_error(p.st, NBH_ERR_DEPTH);
-                return -1;
-            }
-            if (pass == 1) {
-                const unsigned occ = __reduce_or_sync(0xffffffffu, member ? 1u << o : 0u);
-                if (lane < 8 && !((occ >> lane) & 1u)) cell_child(p, t.cell)[lane] = kNull;
-                if (lane == 0) {
-                    p.arrive[t.cell - nbody] = 0;
-                    p.clevel[t.cell - nbody] = t.level;
-                }
-            }
-            // the largest child cell is pushed deepest (popped last); the others above it
-            int pos = 0;
-            if (nc > 1) {
-                const unsigned key = (leader && cnt >= 2) ? ((unsigned)cnt << 5) | (31u - lane) : 0u;
-                const unsigned kmax = __reduce_max_sync(0xffffffffu, key);
-                const int largest = 31 - (int)(kmax & 31u);
-                const unsigned others = balc & ~(1u << largest);
-                pos = lane == largest ? 0 : 1 + __popc(others & lt);
-            }
-            if (leader) {
-                if (cnt == 1) {
-                    if (pass == 1) cell_child(p, t.cell)[o] = b;
-                    local_max = max(local_max, t.level + 1);
-                } else {
-                    const int v = pass == 1 ? base - 1 - made - __popc(balc & lt) : 0;
-                    if (pass == 1) cell_child(p, t.cell)[o] = v;
-                    const float h = t.r * 0.5f;
-                    st[top + pos] = SmallTask{grp, v, t.level + 1,
-                                              __fadd_rn(__fsub_rn(t.cx, h), (o & 1) ? t.r : 0.0f),
-                                              __fadd_rn(__fsub_rn(t.cy, h), (o & 2) ? t.r : 0.0f),
-                                              __fadd_rn(__fsub_rn(t.cz, h), (o & 4) ? t.r : 0.0f), h};
-                }
-            }
-            made += nc;
-            top += nc;
-            __syncwarp();
+        const bool member = (t.mask >> lane) & 1u;
+        const int o = member ? octant(t.cx, t.cy, t.cz, q.x, q.y, q.z) : -1;
+        const unsigned grp = __match_any_sync(0xffffffffu, o);
+        const bool leader = member && (__ffs(grp) - 1) == lane;
+        const int cnt = __popc(grp);
+        const unsigned balc = __ballot_sync(0xffffffffu, leader && cnt >= 2);
+        const int nc = __popc(balc);
+        if (nc > 0 && (t.level + 2 > kMaxDepth || top + nc > kSmallStack)) {   // coincident bodies
+            raise_error(p.st, NBH_ERR_DEPTH);
+            return -1;
         }
-        if (pass == 0) next = made;
-        else return root;
+        if (build) {
+            const unsigned occ = __reduce_or_sync(0xffffffffu, member ? 1u << o : 0u);
+            if (lane < 8 && !((occ >> lane) & 1u)) cell_child(p, t.cell)[lane] = kNull;
+            if (lane == 0) {
+                p.arrive[t.cell - nbody] = 0;
+                p.clevel[t.cell - nbody] = t.level;
+            }
+        }
+        // the largest child cell is pushed deepest (popped last); the others above it
+        int pos = 0;
+        if (nc > 1) {
+            const unsigned key = (leader && cnt >= 2) ? ((unsigned)cnt << 5) | (31u - lane) : 0u;
+            const unsigned kmax = __reduce_max_sync(0xffffffffu, key);
+            const int largest = 31 - (int)(kmax & 31u);
+            const unsigned others = balc & ~(1u << largest);
+            pos = lane == largest ? 0 : 1 + __popc(others & lt);
+        }
+        if (leader) {
+            if (cnt == 1) {
+                if (build) cell_child(p, t.cell)[o] = b;
+                local_max = max(local_max, t.level + 1);
+            } else {
+                const int v = build ? base - 1 - made - __popc(balc & lt) : 0;
+                if (build) cell_child(p, t.cell)[o] = v;
+                const float h = t.r * 0.5f;
+                st[top + pos] = SmallTask{grp, v, t.level + 1,
+                                          __fadd_rn(__fsub_rn(t.cx, h), (o & 1) ? t.r : 0.0f),
+                                          __fadd_rn(__fsub_rn(t.cy, h), (o & 2) ? t.r : 0.0f),
+                                          __fadd_rn(__fsub_rn(t.cz, h), (o & 4) ? t.r : 0.0f), h};
+            }
+        }
+        made += nc;
+        top += nc;
+        __syncwarp();
     }
-    return -1;
+    return build ? root : made;
+}
+
+// Both passes with an allocation of their own in between (the large-bucket path).
+__device__ int build_small(const StepParams& p, const int* __restrict__ src, int lo, int m, int cell, int level,
+                           float cx, float cy, float cz, float r, SmallTask* st, int& local_max) {
+    const int need = small_subtree(p, src, lo, m, cell, level, cx, cy, cz, r, st, local_max, false, 0);
+    if (need < 0) return -1;
+    int base = 0;
+    if (need > 0) {
+        if ((threadIdx.x & 31) == 0) base = atomicSub(&p.st->bottom, need);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base - need <= p.nbody) {
+            raise_error(p.st, NBH_ERR_POOL);
+            return -1;
+        }
+    }
+    return small_subtree(p, src, lo, m, cell, level, cx, cy, cz, r, st, local_max, true, base);
 }
 
 __global__ void __launch_bounds__(32 * kBucketWarps) bucket_build_kernel(StepParams p) {
@@ -576,153 +585,207 @@ __global__ void __launch_bounds__(32 * kBucketWarps) bucket_build_kernel(StepPar
     const int nb = ld_relaxed(&p.st->nbuckets);
     int local_max = 1;
     for (;;) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(&p.st->bucket_next, 1);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= nb) break;
-        const int4 bk = p.buckets[item];
-        const int c = nbody + (bk.x >> 3), j = bk.x & 7;
-        const int start = bk.y, k = bk.z;
-        const int m = k + (bk.w >= 0 ? 1 : 0);
-        if (bk.w >= 0 && lane == 0) p.bwork[start + k] = bk.w;
+        // a chunk of buckets per warp: one atomic hands out kBucketChunk of them
+        int item0 = 0;
+        if (lane == 0) item0 = atomicAdd(&p.st->bucket_next, kBucketChunk);
+        item0 = __shfl_sync(0xffffffffu, item0, 0);
+        if (item0 >= nb) break;
+        const int nitem = min(kBucketChunk, nb - item0);
+        // lane l < nitem holds bucket item0 + l; the body its slot already held joins the
+        // bucket's entries
+        int4 bkt = make_int4(0, 0, 0, kNull);
+        if (lane < nitem) {
+            bkt = p.buckets[item0 + lane];
+            if (bkt.w >= 0) p.bwork[bkt.y + bkt.z] = bkt.w;
+        }
         __syncwarp();
-        // cell c's centre and half-width, recorded by the locate pass
-        const float4 g = reinterpret_cast<const float4*>(bucket_counters(p, c))[4];
-        const int clev = p.clevel[c - nbody];
-        int* slot = cell_child(p, c) + j;
-        if (m == 1) {                                 // a single body: the slot takes it
-            if (lane == 0) *slot = p.bwork[start];
-            local_max = max(local_max, clev + 1);
-            continue;
+        // (A) count the new cells of every bucket of 2..32 bodies, then take them for the whole
+        // chunk with one allocation: bucket l's cells lie below chunk_base minus the cells of
+        // the chunk's buckets before it
+        int need = 0;                                // lane l: cells of bucket l
+        for (int it = 0; it < nitem; ++it) {
+            const int bx = __shfl_sync(0xffffffffu, bkt.x, it), start = __shfl_sync(0xffffffffu, bkt.y, it);
+            const int m = __shfl_sync(0xffffffffu, bkt.z, it) + (__shfl_sync(0xffffffffu, bkt.w, it) >= 0 ? 1 : 0);
+            if (m < 2 || m > 32) continue;
+            const int c = nbody + (bx >> 3), j = bx & 7;
+            const float4 g = reinterpret_cast<const float4*>(bucket_counters(p, c))[4];
+            const int clev = p.clevel[c - nbody];
+            if (clev + 2 > kMaxDepth) {
+                raise_error(p.st, NBH_ERR_DEPTH);
+                return;
+            }
+            const float h0 = g.w * 0.5f;
+            const int cells = small_subtree(p, p.bwork, start, m, -1, clev + 1,
+                                            __fadd_rn(__fsub_rn(g.x, h0), (j & 1) ? g.w : 0.0f),
+                                            __fadd_rn(__fsub_rn(g.y, h0), (j & 2) ? g.w : 0.0f),
+                                            __fadd_rn(__fsub_rn(g.z, h0), (j & 4) ? g.w : 0.0f), h0, sstack,
+                                            local_max, false, 0);
+            if (cells < 0) return;
+            if (lane == it) need = cells;
         }
-        if (clev + 2 > kMaxDepth) {
-            raise_error(p.st, NBH_ERR_DEPTH);
-            return;
+        int incl = need;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
         }
-        // the subtree's root: the child of c in octant j
-        const float h0 = g.w * 0.5f;
-        const float rcx = __fadd_rn(__fsub_rn(g.x, h0), (j & 1) ? g.w : 0.0f);
-        const float rcy = __fadd_rn(__fsub_rn(g.y, h0), (j & 2) ? g.w : 0.0f);
-        const float rcz = __fadd_rn(__fsub_rn(g.z, h0), (j & 4) ? g.w : 0.0f);
-        int root;
-        if (m <= 32) {
-            root = build_small(p, p.bwork, start, m, -1, clev + 1, rcx, rcy, rcz, h0, sstack, local_max);
-            if (root < 0) return;
-            if (lane == 0) *slot = root;
-            continue;
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        int chunk_base = 0;
+        if (total > 0) {
+            if (lane == 0) chunk_base = atomicSub(&p.st->bottom, total);
+            chunk_base = __shfl_sync(0xffffffffu, chunk_base, 0);
+            if (chunk_base - total <= nbody) {
+                raise_error(p.st, NBH_ERR_POOL);
+                return;
+            }
         }
-        if (lane == 0) root = atomicSub(&p.st->bottom, 1) - 1;
-        root = __shfl_sync(0xffffffffu, root, 0);
-        if (root <= nbody) {
-            raise_error(p.st, NBH_ERR_POOL);
-            return;
-        }
-        if (lane == 0) stack[0] = BucketTask{root, clev + 1, start, start + m, 0, rcx, rcy, rcz, h0};
-        int top = 1;
-        __syncwarp();
-        bool ok = true;
-        while (top > 0) {
-            const BucketTask t = stack[--top];
-            __syncwarp();
-            const int* src = p.bwork + (t.buf ? nbody : 0);
-            int* dst = p.bwork + (t.buf ? 0 : nbody);
-            if (t.hi - t.lo <= 32) {                  // small enough for the register builder
-                if (build_small(p, src, t.lo, t.hi - t.lo, t.cell, t.level, t.cx, t.cy, t.cz, t.r, sstack,
-                                local_max) < 0) {
-                    ok = false;
-                    break;
-                }
+        const int my_base = chunk_base - (incl - need);
+        // (B) build each bucket's subtree
+        for (int it = 0; it < nitem; ++it) {
+            const int bx = __shfl_sync(0xffffffffu, bkt.x, it);
+            const int c = nbody + (bx >> 3), j = bx & 7;
+            const int start = __shfl_sync(0xffffffffu, bkt.y, it);
+            const int m = __shfl_sync(0xffffffffu, bkt.z, it) + (__shfl_sync(0xffffffffu, bkt.w, it) >= 0 ? 1 : 0);
+            const int sub_base = __shfl_sync(0xffffffffu, my_base, it);
+            // cell c's centre and half-width, recorded by the locate pass
+            const float4 g = reinterpret_cast<const float4*>(bucket_counters(p, c))[4];
+            const int clev = p.clevel[c - nbody];
+            int* slot = cell_child(p, c) + j;
+            if (m == 1) {                                 // a single body: the slot takes it
+                if (lane == 0) *slot = p.bwork[start];
+                local_max = max(local_max, clev + 1);
                 continue;
             }
-            // pass 1: bodies per octant (lane o < 8 holds octant o's count)
-            int mycnt = 0;
-            for (int base = t.lo; base < t.hi; base += 32) {
-                const int i = base + lane;
-                int o = -1;
-                if (i < t.hi) {
-                    const float4 q = p.node4[src[i]];
-                    o = octant(t.cx, t.cy, t.cz, q.x, q.y, q.z);
-                }
-#pragma unroll
-                for (int oc = 0; oc < 8; ++oc) {
-                    const int n = __popc(__ballot_sync(0xffffffffu, o == oc));
-                    if (lane == oc) mycnt += n;
-                }
+            if (clev + 2 > kMaxDepth) {
+                raise_error(p.st, NBH_ERR_DEPTH);
+                return;
             }
-            // exclusive offsets of the octants (lanes 0..7)
-            int myoff = mycnt;
-#pragma unroll
-            for (int o2 = 1; o2 < 8; o2 <<= 1) {
-                const int v = __shfl_up_sync(0xffffffffu, myoff, o2);
-                if (lane >= o2) myoff += v;
+            // the subtree's root: the child of c in octant j
+            const float h0 = g.w * 0.5f;
+            const float rcx = __fadd_rn(__fsub_rn(g.x, h0), (j & 1) ? g.w : 0.0f);
+            const float rcy = __fadd_rn(__fsub_rn(g.y, h0), (j & 2) ? g.w : 0.0f);
+            const float rcz = __fadd_rn(__fsub_rn(g.z, h0), (j & 4) ? g.w : 0.0f);
+            int root;
+            if (m <= 32) {
+                root = small_subtree(p, p.bwork, start, m, -1, clev + 1, rcx, rcy, rcz, h0, sstack, local_max, true,
+                                     sub_base);
+                if (root < 0) return;
+                if (lane == 0) *slot = root;
+                continue;
             }
-            myoff -= mycnt;
-            // pass 2: bodies to dst in octant order
-            int run = 0;                              // lane o: bodies of octant o placed so far
-            for (int base = t.lo; base < t.hi; base += 32) {
-                const int i = base + lane;
-                int o = -1, b = 0;
-                if (i < t.hi) {
-                    b = src[i];
-                    const float4 q = p.node4[b];
-                    o = octant(t.cx, t.cy, t.cz, q.x, q.y, q.z);
-                }
-                unsigned mine = 0;
-#pragma unroll
-                for (int oc = 0; oc < 8; ++oc) {
-                    const unsigned bal = __ballot_sync(0xffffffffu, o == oc);
-                    if (o == oc) mine = bal;
-                    if (lane == oc) run += __popc(bal);
-                }
-                const int slot_base = __shfl_sync(0xffffffffu, myoff + run, o < 0 ? 0 : o);
-                // slot_base counts this chunk's bodies of octant o already: subtract them
-                if (o >= 0) dst[t.lo + slot_base - __popc(mine) + __popc(mine & lt)] = b;
+            if (lane == 0) root = atomicSub(&p.st->bottom, 1) - 1;
+            root = __shfl_sync(0xffffffffu, root, 0);
+            if (root <= nbody) {
+                raise_error(p.st, NBH_ERR_POOL);
+                return;
             }
+            if (lane == 0) stack[0] = BucketTask{root, clev + 1, start, start + m, 0, rcx, rcy, rcz, h0};
+            int top = 1;
             __syncwarp();
-            // children: empty, one body, or a cell (allocated together)
-            const bool is_cell = lane < 8 && mycnt >= 2;
-            const unsigned balc = __ballot_sync(0xffffffffu, is_cell);
-            const int nc = __popc(balc);
-            int cbase = 0;
-            if (nc > 0) {
-                if (t.level + 2 > kMaxDepth || top + nc > kBucketStack) {   // coincident bodies
-                    raise_error(p.st, NBH_ERR_DEPTH);
-                    ok = false;
-                    break;
+            bool ok = true;
+            while (top > 0) {
+                const BucketTask t = stack[--top];
+                __syncwarp();
+                const int* src = p.bwork + (t.buf ? nbody : 0);
+                int* dst = p.bwork + (t.buf ? 0 : nbody);
+                if (t.hi - t.lo <= 32) {                  // small enough for the register builder
+                    if (build_small(p, src, t.lo, t.hi - t.lo, t.cell, t.level, t.cx, t.cy, t.cz, t.r, sstack,
+                                    local_max) < 0) {
+                        ok = false;
+                        break;
+                    }
+                    continue;
                 }
-                if (lane == 0) cbase = atomicSub(&p.st->bottom, nc);
-                cbase = __shfl_sync(0xffffffffu, cbase, 0);
-                if (cbase - nc <= nbody) {
-                    raise_error(p.st, NBH_ERR_POOL);
-                    ok = false;
-                    break;
+                // pass 1: bodies per octant (lane o < 8 holds octant o's count)
+                int mycnt = 0;
+                for (int base = t.lo; base < t.hi; base += 32) {
+                    const int i = base + lane;
+                    int o = -1;
+                    if (i < t.hi) {
+                        const float4 q = p.node4[src[i]];
+                        o = octant(t.cx, t.cy, t.cz, q.x, q.y, q.z);
+                    }
+#pragma unroll
+                    for (int oc = 0; oc < 8; ++oc) {
+                        const int n = __popc(__ballot_sync(0xffffffffu, o == oc));
+                        if (lane == oc) mycnt += n;
+                    }
                 }
-            }
-            const int deeper = deeper_rank(mycnt, lane);
-            if (lane < 8) {
-                int v = kNull;
-                if (mycnt == 1) {
-                    v = dst[t.lo + myoff];
-                    local_max = max(local_max, t.level + 1);
-                } else if (mycnt >= 2) {
-                    v = cbase - 1 - __popc(balc & lt);
-                    const float h = t.r * 0.5f;
-                    stack[top + deeper] = BucketTask{v, t.level + 1, t.lo + myoff, t.lo + myoff + mycnt, t.buf ^ 1,
-                                                     __fadd_rn(__fsub_rn(t.cx, h), (lane & 1) ? t.r : 0.0f),
-                                                     __fadd_rn(__fsub_rn(t.cy, h), (lane & 2) ? t.r : 0.0f),
-                                                     __fadd_rn(__fsub_rn(t.cz, h), (lane & 4) ? t.r : 0.0f), h};
+                // exclusive offsets of the octants (lanes 0..7)
+                int myoff = mycnt;
+#pragma unroll
+                for (int o2 = 1; o2 < 8; o2 <<= 1) {
+                    const int v = __shfl_up_sync(0xffffffffu, myoff, o2);
+                    if (lane >= o2) myoff += v;
                 }
-                cell_child(p, t.cell)[lane] = v;
+                myoff -= mycnt;
+                // pass 2: bodies to dst in octant order
+                int run = 0;                              // lane o: bodies of octant o placed so far
+                for (int base = t.lo; base < t.hi; base += 32) {
+                    const int i = base + lane;
+                    int o = -1, b = 0;
+                    if (i < t.hi) {
+                        b = src[i];
+                        const float4 q = p.node4[b];
+                        o = octant(t.cx, t.cy, t.cz, q.x, q.y, q.z);
+                    }
+                    unsigned mine = 0;
+#pragma unroll
+                    for (int oc = 0; oc < 8; ++oc) {
+                        const unsigned bal = __ballot_sync(0xffffffffu, o == oc);
+                        if (o == oc) mine = bal;
+                        if (lane == oc) run += __popc(bal);
+                    }
+                    const int slot_base = __shfl_sync(0xffffffffu, myoff + run, o < 0 ? 0 : o);
+                    // slot_base counts this chunk's bodies of octant o already: subtract them
+                    if (o >= 0) dst[t.lo + slot_base - __popc(mine) + __popc(mine & lt)] = b;
+                }
+                __syncwarp();
+                // children: empty, one body, or a cell (allocated together)
+                const bool is_cell = lane < 8 && mycnt >= 2;
+                const unsigned balc = __ballot_sync(0xffffffffu, is_cell);
+                const int nc = __popc(balc);
+                int cbase = 0;
+                if (nc > 0) {
+                    if (t.level + 2 > kMaxDepth || top + nc > kBucketStack) {   // coincident bodies
+                        raise_error(p.st, NBH_ERR_DEPTH);
+                        ok = false;
+                        break;
+                    }
+                    if (lane == 0) cbase = atomicSub(&p.st->bottom, nc);
+                    cbase = __shfl_sync(0xffffffffu, cbase, 0);
+                    if (cbase - nc <= nbody) {
+                        raise_error(p.st, NBH_ERR_POOL);
+                        ok = false;
+                        break;
+                    }
+                }
+                const int deeper = deeper_rank(mycnt, lane);
+                if (lane < 8) {
+                    int v = kNull;
+                    if (mycnt == 1) {
+                        v = dst[t.lo + myoff];
+                        local_max = max(local_max, t.level + 1);
+                    } else if (mycnt >= 2) {
+                        v = cbase - 1 - __popc(balc & lt);
+                        const float h = t.r * 0.5f;
+                        stack[top + deeper] = BucketTask{v, t.level + 1, t.lo + myoff, t.lo + myoff + mycnt, t.buf ^ 1,
+                                                         __fadd_rn(__fsub_rn(t.cx, h), (lane & 1) ? t.r : 0.0f),
+                                                         __fadd_rn(__fsub_rn(t.cy, h), (lane & 2) ? t.r : 0.0f),
+                                                         __fadd_rn(__fsub_rn(t.cz, h), (lane & 4) ? t.r : 0.0f), h};
+                    }
+                    cell_child(p, t.cell)[lane] = v;
+                }
+                if (lane == 0) {
+                    p.arrive[t.cell - nbody] = 0;
+                    p.clevel[t.cell - nbody] = t.level;
+                }
+                top += nc;
+                __syncwarp();
             }
-            if (lane == 0) {
-                p.arrive[t.cell - nbody] = 0;
-                p.clevel[t.cell - nbody] = t.level;
-            }
-            top += nc;
-            __syncwarp();
+            if (!ok) return;
+            if (lane == 0) *slot = root;
         }
-        if (!ok) return;
-        if (lane == 0) *slot = root;
     }
     // :199; the maximum persists across steps, so the atomic is rarely needed
 #pragma unroll
