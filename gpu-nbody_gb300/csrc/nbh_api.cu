@@ -1132,7 +1132,9 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
         StepParams q = step_params(sim);
         q.theta_body = nullptr;
         q.probe = sim->probe;           // results go to the scratch buffer, body state untouched
-        q.item_order = nullptr;         // index order (the step's order belongs to its own width)
+        // the steps' own order of the work items (longest walks first) where it belongs to this
+        // width, else index order; the trials record no costs
+        q.item_order = (vote == sim->order_vote) ? sim->item_order : nullptr;
         q.item_cost = nullptr;
         q.stack_cap = g.second;
         const int grid = occ * sim->sms;

@@ -148,9 +148,10 @@ def test_tree_matches_oracle_and_invariants():
     assert root[0] == ot["x"][o.nn] and root[1] == ot["y"][o.nn] and root[2] == ot["z"][o.nn]
 
 
-def _reachable_bodies(t, n):
-    """Bodies reachable from the root through the child slots, level by level."""
-    child, front, out = t["child"], np.array([t["nnodes"]]), []
+def _reachable_bodies(t, n, roots=None):
+    """Bodies reachable from the root(s) through the child slots, level by level."""
+    child, out = t["child"], []
+    front = np.array([t["nnodes"]]) if roots is None else np.asarray(roots)
     while front.size:
         ch = child[front - n].ravel()
         out.append(ch[(ch >= 0) & (ch < n)])
@@ -406,6 +407,42 @@ def test_step_io_equals_write_step_read():
         g.step_io(1, write={"x": hin["x"]})           # positions need x, y and z
     assert ei.value.code == L.NBH_ERR_INVALID
     g.close()
+
+
+def test_batch_rebuilds_under_contention_hold_every_body_and_repeat():
+    """A batch of 192 Plummer universes (1 to 40,000 bodies, 625,654 in all) with dt = 0, built in
+    one lock pass (every universe's bodies contend in its top levels at once) and with the
+    default schedule: every rebuild reaches every body once from its own universe's root,
+    and repeats the depth-first order and the accelerations bit for bit."""
+    from nbh import universe as U
+    rng = np.random.default_rng(11)
+    counts = np.exp(rng.uniform(0.0, np.log(40000), 192)).astype(np.int32)
+    counts[:3] = (1, 2, 40000)
+    parts = [U.PlummerUniverseGenerator(seed=300 + i).arrays(int(c)) for i, c in enumerate(counts)]
+    cat = [np.concatenate([p[k] for p in parts]) for k in range(7)]
+    n = int(counts.sum())
+    off = np.concatenate([[0], np.cumsum(counts)])
+    ref = None
+    for phases, buckets in ((1, 2), (5, 1)):
+        g = gpu_sim(theta=0.5, eps=0.05, dt=0.0, vote_width=64, build_phases=phases, build_buckets=buckets)
+        g.load_batch(counts, *cat)
+        for s in range(4):
+            g.step()
+            t = g.tree()
+            where = "schedule %d/%d rebuild %d" % (phases, buckets, s)
+            reach = _reachable_bodies(t, n, t["roots"])
+            assert reach.size == n and np.unique(reach).size == n, where
+            for u in (0, 1, 2, 100):      # each body hangs below its own universe's root
+                ru = _reachable_bodies(t, n, [t["roots"][u]])
+                assert np.array_equal(np.sort(ru), np.arange(off[u], off[u + 1])), (where, u)
+            st = g.read()
+            acc = np.stack([st["ax"], st["ay"], st["az"]])
+            if ref is None:
+                ref = (t["sorted"].copy(), acc)
+            else:
+                np.testing.assert_array_equal(t["sorted"], ref[0], err_msg=where)
+                np.testing.assert_array_equal(acc, ref[1], err_msg=where)
+        g.close()
 
 
 def test_massless_tracers_match_oracle():
