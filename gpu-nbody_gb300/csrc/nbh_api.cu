@@ -70,6 +70,9 @@ struct nbh_sim {
     // host mirrors
     DevState* h_state = nullptr;   // pinned
     cudaEvent_t ev[7] = {};
+    // nbh_step_io: velocities and accelerations go up on io_stream while the tree stages run
+    cudaStream_t io_stream = nullptr;
+    cudaEvent_t io_start = nullptr, io_ready = nullptr;
     float stage_ms[7] = {};
     bool loaded = false;
     int64_t steps = 0;
@@ -205,8 +208,11 @@ void ensure_item_order(nbh_sim* sim) {
     sim->order_vote = sim->cfg.vote_width;
 }
 
-// Enqueue the six stages of one step (GPUBarnesHutNBodySimulation.java:258-263).
-void enqueue_step(nbh_sim* sim, bool timed) {
+// Enqueue the six stages of one step (GPUBarnesHutNBodySimulation.java:258-263).  With
+// `vel_acc_ready`, the stages from the angle features on (the first to read velocities or
+// accelerations) wait for that event and first pack the staged components `staged_mask`
+// (2 velocities, 4 accelerations) into the state; the tree stages need positions only.
+void enqueue_step(nbh_sim* sim, bool timed, cudaEvent_t vel_acc_ready = nullptr, int staged_mask = 0) {
     const StepParams p = step_params(sim);
     const bool ref = sim->cfg.arith == NBH_ARITH_REFERENCE;
     cudaStream_t s = sim->stream;
@@ -219,6 +225,11 @@ void enqueue_step(nbh_sim* sim, bool timed) {
     launch_summarize(p, ref, sim->grid_sum, s);
     if (timed) cudaEventRecord(sim->ev[3], s);
     launch_sort(p, sim->grid_sort, s);
+    if (vel_acc_ready) {
+        cudaStreamWaitEvent(s, vel_acc_ready, 0);
+        launch_pack(sim->nbody, sim->staging, staged_mask, sim->node4, sim->vel, sim->acc,
+                    std::max(1, std::min((sim->nbody + 255) / 256, 4 * sim->sms)), s);
+    }
     if (sim->theta_active) launch_theta(p, sim->model, sim->theta_body, sim->grid_force, s);
     if (timed) cudaEventRecord(sim->ev[4], s);
     if (sim->theta_active && sim->theta_every > 1) {
@@ -583,6 +594,10 @@ int nbh_destroy(nbh_sim* sim) {
     if (sim->h_state) cudaFreeHost(sim->h_state);
     for (auto& ev : sim->ev)
         if (ev) cudaEventDestroy(ev);
+    if (sim->io_stream) cudaStreamSynchronize(sim->io_stream);
+    if (sim->io_start) cudaEventDestroy(sim->io_start);
+    if (sim->io_ready) cudaEventDestroy(sim->io_ready);
+    if (sim->io_stream) cudaStreamDestroy(sim->io_stream);
     if (sim->stream) cudaStreamDestroy(sim->stream);
     delete sim;
     return NBH_OK;
@@ -754,14 +769,29 @@ int enqueue_read(nbh_sim* sim, float* const dst[9]) {
     return NBH_OK;
 }
 
-// nbh_write without the wait (same checks and the same two paths as enqueue_read).
-int enqueue_write(nbh_sim* sim, const float* const in[9]) {
+// Each of the three groups of a write is given whole or not at all.
+int check_write_groups(nbh_sim* sim, const float* const in[9]) {
     if ((in[0] || in[1] || in[2]) && !(in[0] && in[1] && in[2]))
         return fail(sim, NBH_ERR_INVALID, "positions need x, y and z");
     if ((in[3] || in[4] || in[5]) && !(in[3] && in[4] && in[5]))
         return fail(sim, NBH_ERR_INVALID, "velocities need vx, vy and vz");
     if ((in[6] || in[7] || in[8]) && !(in[6] && in[7] && in[8]))
         return fail(sim, NBH_ERR_INVALID, "accelerations need ax, ay and az");
+    return NBH_OK;
+}
+
+int ensure_io_stream(nbh_sim* sim) {
+    if (sim->io_stream) return NBH_OK;
+    CK(cudaStreamCreateWithFlags(&sim->io_stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&sim->io_start, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&sim->io_ready, cudaEventDisableTiming));
+    return NBH_OK;
+}
+
+// nbh_write without the wait (same checks and the same two paths as enqueue_read).
+int enqueue_write(nbh_sim* sim, const float* const in[9]) {
+    int e0 = check_write_groups(sim, in);
+    if (e0) return e0;
     const int n = sim->nbody;
     const float* src[10];
     for (int k = 0; k < 9; ++k) src[k] = in[k];
@@ -822,11 +852,41 @@ int nbh_step_io(nbh_sim* sim, int32_t nsteps, const nbh_host_state* in, const nb
     if (nsteps < 0) return fail(sim, NBH_ERR_INVALID, "nsteps < 0");
     CK(cudaSetDevice(sim->device));
     int e;
+    int rest = nsteps;
     if (in) {
         const float* const src[9] = {in->x, in->y, in->z, in->vx, in->vy, in->vz, in->ax, in->ay, in->az};
-        if ((e = enqueue_write(sim, src))) return e;
+        if ((e = check_write_groups(sim, src))) return e;
+        const int n = sim->nbody;
+        HostArrays h;
+        if ((src[3] || src[6]) && nsteps > 0 && mapped_host_views(src, n, &h)) {
+            // Velocities and accelerations are first read by the angle features / the force
+            // walk, after the tree stages.  The positions go up first, alone on the host link
+            // (the tree waits for them); then the copy engines bring velocities and
+            // accelerations into the staging buffer on io_stream while the tree is built,
+            // and the first step waits for them, and packs them, only before those stages.
+            // Copies rather than the in-place kernel: a kernel waiting on host memory would
+            // hold SMs the tree stages need.
+            if ((e = ensure_io_stream(sim))) return e;
+            if (src[0]) launch_pack_host(n, h, 1, sim->node4, sim->vel, sim->acc, std::max(1, (n + 255) / 256),
+                                         sim->stream);
+            CK(cudaGetLastError());
+            CK(cudaEventRecord(sim->io_start, sim->stream));      // positions in, staging free
+            CK(cudaStreamWaitEvent(sim->io_stream, sim->io_start, 0));
+            for (int k = 3; k < 9; ++k)
+                if (src[k])
+                    CK(cudaMemcpyAsync(sim->staging + (size_t)k * n, src[k], sizeof(float) * n,
+                                       cudaMemcpyHostToDevice, sim->io_stream));
+            CK(cudaEventRecord(sim->io_ready, sim->io_stream));
+            ensure_item_order(sim);
+            enqueue_step(sim, sim->cfg.stage_timing != 0, sim->io_ready, (src[3] ? 2 : 0) | (src[6] ? 4 : 0));
+            CK(cudaGetLastError());
+            sim->steps += 1;
+            rest -= 1;
+        } else if ((e = enqueue_write(sim, src))) {
+            return e;
+        }
     }
-    if ((e = nbh_step_async(sim, nsteps))) return e;
+    if ((e = nbh_step_async(sim, rest))) return e;
     CK(cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, sim->stream));
     if (out) {
         float* const dst[9] = {out->x, out->y, out->z, out->vx, out->vy, out->vz, out->ax, out->ay, out->az};

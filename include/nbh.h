@@ -170,8 +170,10 @@ typedef struct nbh_host_state {
 /* For a host that owns the state between steps: writes `in` like nbh_write (in may be
  * NULL), runs nsteps steps like nbh_step, reads the state into `out` like nbh_read (out
  * may be NULL), and waits once at the end instead of after each of the three calls.
- * Pinned (mapped) arrays are read and written in place by the packing kernels.  Returns
- * what nbh_step would. */
+ * Pinned (mapped) arrays are read and written in place by the packing kernels; with pinned
+ * input, velocities and accelerations are copied in on a second stream while the first
+ * step builds its tree from the positions.  Results equal nbh_write + nbh_step + nbh_read.
+ * Returns what nbh_step would. */
 int nbh_step_io(nbh_sim* sim, int32_t nsteps, const nbh_host_state* in, const nbh_host_state* out);
 
 int nbh_get_stats(nbh_sim* sim, nbh_stats* out);

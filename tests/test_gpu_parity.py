@@ -387,6 +387,21 @@ def test_step_io_equals_write_step_read():
         for k in keys:
             np.testing.assert_array_equal(out[k], want[k], err_msg="%s pinned=%s" % (k, pinned))
         g.close()
+    # velocities and accelerations alone (pinned: they go up beside the tree stages)
+    vin = {k: torch.empty(n, dtype=torch.float32, pin_memory=True).numpy() for k in keys[3:]}
+    for k in keys[3:]:
+        vin[k][:] = hin[k]
+    g = fresh()
+    g.write(None, None, None, *[hin[k] for k in keys[3:]])
+    g.step(2)
+    want_v = g.read()
+    g.close()
+    g = fresh()
+    g.step_io(2, write=vin)
+    got_v = g.read()
+    for k in keys:
+        np.testing.assert_array_equal(got_v[k], want_v[k], err_msg="velocity-only write: %s" % k)
+    g.close()
     # write only, then read only; positions only leave the rest as they were
     g = fresh()
     g.step_io(0, write={k: hin[k] for k in keys})
