@@ -53,8 +53,9 @@ def graph_launches(build_phases=5, build_buckets=1):
 FLOPS_PER_INTERACTION = 20          # 3 sub, 3 fma (d^2+eps^2), rsqrt, 3 mul, 3 fma, ~7 more
 HBM_FALLBACK_GBS = 6800.0
 # DRAM bytes (read + write) of one force launch (vote width 64) on the 1,048,576-body
-# Plummer workload, from the ncu capture summarised in profiles/force_kernel_plummer1M.md.
-FORCE_TRAFFIC_BYTES_1M = 211_056_640 + 25_430_016
+# Plummer workload, from one full ncu capture of that launch (dram__bytes_read.sum +
+# dram__bytes_write.sum).
+FORCE_TRAFFIC_BYTES_1M = 206_981_120 + 24_052_480
 
 # Algorithmic bytes per body / per cell of the memory-bound stages (minimum traffic:
 # every byte read and written once).
@@ -466,8 +467,8 @@ def main():
                 "peak": fp32.value, "unit": "TFLOP/s", "frac": achieved / fp32.value,
                 "traffic": FORCE_TRAFFIC_BYTES_1M if (args.workload == "plummer" and n == 1 << 20
                                                       and args.vote_width == DEFAULT_VOTE) else None,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
-                                  "(profiles/force_kernel_plummer1M.md)",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one force "
+                                  "launch of this workload (full capture)",
                 "flops_per_interaction": FLOPS_PER_INTERACTION,
                 "peak_source": "measured FP32 FMA loop on this GPU (nbh_measure_fp32_peak); "
                                "MEASURED_PEAKS.json holds only HBM and bf16 peaks",
