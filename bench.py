@@ -140,7 +140,8 @@ class ClockSampler:
 WORKLOADS = {
     "plummer": {"n": 1 << 20, "dt": 0.01, "precise": False,
                 "what": "Plummer sphere a=1 M=1, equal masses, DF velocities"},
-    "ball": {"n": 16384, "dt": 0.025, "precise": False,
+    # 16K bodies make only 256 groups of 64: the tuner may pick a narrower vote (more groups)
+    "ball": {"n": 16384, "dt": 0.025, "precise": False, "tune_vote": True,
              "what": "uniform unit ball, equal masses 1/N, Gaussian velocities sigma 0.05"},
     "disc": {"n": 1 << 22, "dt": 0.01, "precise": True,
              "what": "exponential disc rd=1 zd=0.1 (near-circular velocities) + central mass 0.1 "
@@ -348,6 +349,7 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
+    args.tune_vote = args.tune_vote or bool(w.get("tune_vote"))
     if args.n is None:
         args.n = w["n"]
     if args.dt is None:
