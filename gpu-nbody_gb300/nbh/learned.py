@@ -7,8 +7,8 @@ sum, and the target of a body is the largest angle whose error stays within `tau
 interpolation between grid angles).  Samples pair the features measured in the probe at
 each grid angle with that target.  Training runs on the GPU (nbh_mlp_train: FP32 forward
 and backward kernels, Adam) with a pinball loss at a low quantile, so that the predicted
-angle errs on the safe side.  The fixed-angle walk stays the fallback and the judge of the
-error: every evaluation measures the error against FP64.
+angle errs on the safe side.  The fixed-angle walk stays the fallback and the yardstick of
+the error: every evaluation measures the error against FP64.
 """
 from __future__ import annotations
 
