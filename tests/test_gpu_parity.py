@@ -460,6 +460,26 @@ def test_batch_rebuilds_under_contention_hold_every_body_and_repeat():
         g.close()
 
 
+def test_long_run_keeps_every_tree_whole():
+    """200 steps of a moving 1M-body Plummer sphere (autotuned geometry, default schedule):
+    every 50 steps the tree reaches each body once from the root, the depth-first order is a
+    permutation, the state is finite and the step reports no error."""
+    n = 1 << 20
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    g.load(*plummer(n, seed=3))
+    g.autotune()
+    for s in range(4):
+        g.step(50)
+        t = g.tree()
+        reach = _reachable_bodies(t, n)
+        assert reach.size == n and np.unique(reach).size == n, s
+        assert np.array_equal(np.sort(t["sorted"]), np.arange(n)), s
+        st = g.read()
+        assert all(np.isfinite(st[k]).all() for k in KEYS), s
+        assert g.stats()["status"] == 0
+    g.close()
+
+
 def test_massless_tracers_match_oracle():
     """A quarter of the bodies carry no mass (tracers).  Cells holding only tracers have no
     defined centre of mass (0/0, as in the reference's summarize), never pass the opening
