@@ -843,6 +843,59 @@ __device__ __forceinline__ int arrive_acq_rel(int* p) {
     return old;
 }
 
+// One cell's children, in slot order: compacts the slots and writes each child's record into
+// the cell's kids4 block, records each child cell's offset (loff) and the cell's body count,
+// and returns the centre of mass and mass -- summed in FP32 (F64 = false) or, for a root in
+// precise mode, in FP64.
+template <bool REF, bool F64>
+__device__ __forceinline__ float4 sum_children(const StepParams& p, int c, const int (&sl)[8], int* ch8) {
+    const int nbody = p.nbody;
+    int used = 0, cnt = 0;
+    float cm = 0.0f, sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    double dm = 0.0, dx = 0.0, dy = 0.0, dz = 0.0;
+    float4* kb = p.kids4 + ((size_t)(c - nbody) << 3);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int ch = sl[j];
+        if (ch < 0) continue;
+        const float4 q = ld_cg4(p.node4 + ch);
+        if (ch >= nbody) {
+            p.loff[ch - nbody] = cnt;
+            cnt += __ldcg(p.count + (ch - nbody));
+        } else {
+            cnt += 1;
+        }
+        if constexpr (F64) {
+            dm += (double)q.w;
+            dx += (double)q.x * (double)q.w;
+            dy += (double)q.y * (double)q.w;
+            dz += (double)q.z * (double)q.w;
+        } else {
+            cm = __fadd_rn(cm, q.w);
+            sx = madd<REF>(q.x, q.w, sx);
+            sy = madd<REF>(q.y, q.w, sy);
+            sz = madd<REF>(q.z, q.w, sz);
+        }
+        // compacted slot and the child's record, at the running position
+        ch8[used] = ch;
+        kb[used] = q;
+        ++used;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (j >= used) {
+            ch8[j] = kNull;
+            kb[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    p.count[c - nbody] = cnt;
+    if constexpr (F64) {
+        return make_float4((float)(dx / dm), (float)(dy / dm), (float)(dz / dm), (float)dm);
+    } else {
+        const float inv = __fdiv_rn(1.0f, cm);
+        return make_float4(__fmul_rn(sx, inv), __fmul_rn(sy, inv), __fmul_rn(sz, inv), cm);
+    }
+}
+
 template <bool REF, bool PRECISE>
 __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
     if (load_status(p.st)) return;
@@ -862,51 +915,11 @@ __global__ void __launch_bounds__(256) summarize_kernel(StepParams p) {
             const int4 s0 = reinterpret_cast<const int4*>(ch8)[0];
             const int4 s1 = reinterpret_cast<const int4*>(ch8)[1];
             const int sl[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
-            int used = 0, cnt = 0;
-            float cm = 0.0f, sx = 0.0f, sy = 0.0f, sz = 0.0f;
-            double dm = 0.0, dx = 0.0, dy = 0.0, dz = 0.0;
-            const bool froot = PRECISE && c >= first_root;
-            float4* kb = p.kids4 + ((size_t)(c - nbody) << 3);
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int ch = sl[j];
-                if (ch < 0) continue;
-                const float4 q = ld_cg4(p.node4 + ch);
-                if (ch >= nbody) {
-                    p.loff[ch - nbody] = cnt;
-                    cnt += __ldcg(p.count + (ch - nbody));
-                } else {
-                    cnt += 1;
-                }
-                if (froot) {
-                    dm += (double)q.w;
-                    dx += (double)q.x * (double)q.w;
-                    dy += (double)q.y * (double)q.w;
-                    dz += (double)q.z * (double)q.w;
-                } else {
-                    cm = __fadd_rn(cm, q.w);
-                    sx = madd<REF>(q.x, q.w, sx);
-                    sy = madd<REF>(q.y, q.w, sy);
-                    sz = madd<REF>(q.z, q.w, sz);
-                }
-                // compacted slot and the child's record, at the running position
-                ch8[used] = ch;
-                kb[used] = q;
-                ++used;
-            }
-#pragma unroll
-            for (int j = 0; j < 8; ++j)
-                if (j >= used) {
-                    ch8[j] = kNull;
-                    kb[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-            p.count[c - nbody] = cnt;
-            if (froot) {
-                p.node4[c] = make_float4((float)(dx / dm), (float)(dy / dm), (float)(dz / dm), (float)dm);
-            } else {
-                const float inv = __fdiv_rn(1.0f, cm);
-                p.node4[c] = make_float4(__fmul_rn(sx, inv), __fmul_rn(sy, inv), __fmul_rn(sz, inv), cm);
-            }
+            // (precise mode: the roots in FP64, as a path of its own -- folded into the
+            // FP32 loop as a per-child branch, it ran the FP64 arithmetic for every cell)
+            const float4 com = (PRECISE && c >= first_root) ? sum_children<REF, true>(p, c, sl, ch8)
+                                                            : sum_children<REF, false>(p, c, sl, ch8);
+            p.node4[c] = com;
             const int pc = p.parent[c];
             if (pc < 0) break;          // a root
             if (pc <= c) {              // parents always have higher indices
