@@ -50,7 +50,7 @@ struct nbh_sim {
     int force_threads = 128;       // force launch geometry (nbh_autotune)
     int stack_cap = 256;
     int build_phases = 5;          // octree insertion launches
-    bool build_buckets = true;     // lock phases insert a 1/16 sample, the rest is built per slot
+    bool build_buckets = true;     // lock phases insert a sample, the rest is built per slot
     int4* buckets = nullptr;       // bucketed build: nbody records
     int* bwork = nullptr;          // bucketed build: 2 * nbody entries
     unsigned char* bstack = nullptr;   // bucketed build: per-warp task stacks

@@ -7,8 +7,9 @@ namespace nbh {
 struct StepParams;
 
 void launch_bbox(const StepParams& p, int grid, cudaStream_t s);
-// 1, 3 or 5 lock insertion phases; with `buckets` (3 or 5 phases) the lock phases insert a
-// 1/16 sample and the rest is built as lock-free subtrees, one per slot of the sample tree
+// 1, 3 or 5 lock insertion phases; with `buckets` the lock phases (5: three of them; 3: one,
+// of 1/256) insert the sample and the rest is built as lock-free subtrees, one per slot of
+// the tree so far (3: two such passes, the first completing the 1/16 sample)
 void launch_build(const StepParams& p, int phases, bool buckets, int sms, cudaStream_t s);
 size_t bucket_stack_bytes(int sms);   // global task stacks of the bucketed build's grid
 void launch_link(const StepParams& p, int grid, cudaStream_t s);

@@ -311,9 +311,10 @@ finish:
 }
 
 // -------------------------------------------------------------------------------------
-// Bucketed completion of the build.  After the lock phases have inserted a 1/16 sample
-// of every chunk (the "sampled tree"), each remaining body finds, by a read-only descent,
-// the slot of the sampled tree it would be inserted into.  The bodies headed for one slot
+// Bucketed completion of the build.  After the lock phases have inserted a sample of every
+// chunk (the "sampled tree": 1/16, or 1/256 before a first pass that completes the 1/16
+// sample the same way), each remaining body of the pass finds, by a read-only descent, the
+// slot of the sampled tree it would be inserted into.  The bodies headed for one slot
 // (its bucket, plus the body already in it) are exactly those of the subtree that replaces
 // the slot in the final tree, and no other body touches that subtree, so one warp builds
 // it alone: no locks, no release fences (later kernels read it across the kernel
@@ -322,8 +323,11 @@ finish:
 // centres (the same arithmetic from the same parent centre and half-width).
 //
 // Bucket counters of a sampled-tree cell live in its kids4 block, which summarize
-// overwrites later in the step: ints 0..7 = bodies headed for slot j, 8..15 = first entry
-// of slot j's bucket in the work list, 16..19 = the cell's centre and half-width.
+// overwrites later in the step: ints 0..7 = bodies headed for slot j (zeroed when the cell
+// is made; the scatter counts them back to zero, so a second pass starts from zero too),
+// 8..15 = first entry of slot j's bucket in the work list (written by the allocation for
+// every slot with bodies before the scatter reads it), 16..19 = the cell's centre and
+// half-width.
 __device__ __forceinline__ int* bucket_counters(const StepParams& p, int c) {
     return reinterpret_cast<int*>(p.kids4 + ((size_t)(c - p.nbody) << 3));
 }
@@ -331,14 +335,20 @@ constexpr BuildPhase kBucketBodies = {1, 16};   // the bodies outside the 1/16 s
 
 // (1) locate: read-only descent of each remaining body to its slot; the slot index goes
 // to parent[b] (scratch: the link pass writes the body's parent later).
-__global__ void __launch_bounds__(256) bucket_locate_kernel(StepParams p) {
+__global__ void __launch_bounds__(256) bucket_locate_kernel(StepParams p, BuildPhase set, bool reset_counters) {
     if (load_status(p.st)) return;
+    if (reset_counters && blockIdx.x == 0 && threadIdx.x == 0) {
+        // a second pass: the work-list counters start over (the first pass is complete)
+        p.st->bucket_fill = 0;
+        p.st->nbuckets = 0;
+        p.st->bucket_next = 0;
+    }
     const int nbody = p.nbody;
-    const int per = phase_bodies(kBucketBodies);
+    const int per = phase_bodies(set);
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= (long long)p.nchunks * per) return;
     const int4 ck = p.chunks[g / per];
-    const int b = ck.y + phase_offset(kBucketBodies, (int)(g % per), g / per);
+    const int b = ck.y + phase_offset(set, (int)(g % per), g / per);
     if (b >= ck.z) return;
     const int root = p.nnodes - ck.x;
     const float4 rc = p.node4[root];
@@ -376,62 +386,67 @@ __global__ void __launch_bounds__(256) bucket_locate_kernel(StepParams p) {
 __global__ void __launch_bounds__(256) bucket_alloc_kernel(StepParams p) {
     if (load_status(p.st)) return;
     const int nbody = p.nbody;
-    const int c = ld_relaxed(&p.st->bottom) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const bool valid = c <= p.nnodes;
-    int cnt[8], held[8];
-    int total = 0, nb = 0;
-    if (valid) {
-        const int4* bc = reinterpret_cast<const int4*>(bucket_counters(p, c));
-        const int4 a0 = bc[0], a1 = bc[1];
-        const int4* ch = reinterpret_cast<const int4*>(cell_child(p, c));
-        const int4 s0 = ch[0], s1 = ch[1];
-        const int cc[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-        const int ss[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+    const int bottom = ld_relaxed(&p.st->bottom);
+    // block-uniform stride over every cell of the tree so far (the grid is sized for the
+    // usual count; chains of single-child cells between close bodies can exceed it)
+    for (int base = bottom + (int)(blockIdx.x * blockDim.x); base <= p.nnodes; base += (int)(gridDim.x * blockDim.x)) {
+        const int c = base + (int)threadIdx.x;
+        const bool valid = c <= p.nnodes;
+        int cnt[8], held[8];
+        int total = 0, nb = 0;
+        if (valid) {
+            const int4* bc = reinterpret_cast<const int4*>(bucket_counters(p, c));
+            const int4 a0 = bc[0], a1 = bc[1];
+            const int4* ch = reinterpret_cast<const int4*>(cell_child(p, c));
+            const int4 s0 = ch[0], s1 = ch[1];
+            const int cc[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const int ss[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                cnt[j] = cc[j];
+                held[j] = (cc[j] > 0 && ss[j] >= 0 && ss[j] < nbody) ? ss[j] : kNull;
+                total += cc[j] > 0 ? cc[j] + (held[j] >= 0 ? 1 : 0) : 0;
+                nb += cc[j] > 0 ? 1 : 0;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) cnt[j] = 0, held[j] = kNull;
+        }
+        // warp-aggregated allocation of entries and bucket records
+        const int lane = threadIdx.x & 31;
+        int te = total, tb = nb;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int ue = __shfl_up_sync(0xffffffffu, te, o), ub = __shfl_up_sync(0xffffffffu, tb, o);
+            if (lane >= o) te += ue, tb += ub;
+        }
+        int be = 0, bb = 0;
+        if (lane == 31) {
+            be = atomicAdd(&p.st->bucket_fill, te);
+            bb = atomicAdd(&p.st->nbuckets, tb);
+        }
+        be = __shfl_sync(0xffffffffu, be, 31) + te - total;
+        bb = __shfl_sync(0xffffffffu, bb, 31) + tb - nb;
+        if (!valid || total == 0) continue;
+        int* bcw = bucket_counters(p, c);
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            cnt[j] = cc[j];
-            held[j] = (cc[j] > 0 && ss[j] >= 0 && ss[j] < nbody) ? ss[j] : kNull;
-            total += cc[j] > 0 ? cc[j] + (held[j] >= 0 ? 1 : 0) : 0;
-            nb += cc[j] > 0 ? 1 : 0;
+            if (cnt[j] <= 0) continue;
+            bcw[8 + j] = be;
+            p.buckets[bb++] = make_int4(((c - nbody) << 3) | j, be, cnt[j], held[j]);
+            be += cnt[j] + (held[j] >= 0 ? 1 : 0);
         }
-    } else {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) cnt[j] = 0, held[j] = kNull;
-    }
-    // warp-aggregated allocation of entries and bucket records
-    const int lane = threadIdx.x & 31;
-    int te = total, tb = nb;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int ue = __shfl_up_sync(0xffffffffu, te, o), ub = __shfl_up_sync(0xffffffffu, tb, o);
-        if (lane >= o) te += ue, tb += ub;
-    }
-    int be = 0, bb = 0;
-    if (lane == 31) {
-        be = atomicAdd(&p.st->bucket_fill, te);
-        bb = atomicAdd(&p.st->nbuckets, tb);
-    }
-    be = __shfl_sync(0xffffffffu, be, 31) + te - total;
-    bb = __shfl_sync(0xffffffffu, bb, 31) + tb - nb;
-    if (!valid || total == 0) return;
-    int* bcw = bucket_counters(p, c);
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        if (cnt[j] <= 0) continue;
-        bcw[8 + j] = be;
-        p.buckets[bb++] = make_int4(((c - nbody) << 3) | j, be, cnt[j], held[j]);
-        be += cnt[j] + (held[j] >= 0 ? 1 : 0);
     }
 }
 
 // (3) scatter: each remaining body takes an entry of its slot's bucket.
-__global__ void __launch_bounds__(256) bucket_scatter_kernel(StepParams p) {
+__global__ void __launch_bounds__(256) bucket_scatter_kernel(StepParams p, BuildPhase set) {
     if (load_status(p.st)) return;
-    const int per = phase_bodies(kBucketBodies);
+    const int per = phase_bodies(set);
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= (long long)p.nchunks * per) return;
     const int4 ck = p.chunks[g / per];
-    const int b = ck.y + phase_offset(kBucketBodies, (int)(g % per), g / per);
+    const int b = ck.y + phase_offset(set, (int)(g % per), g / per);
     if (b >= ck.z) return;
     const int slot = p.parent[b];
     int* bc = bucket_counters(p, p.nbody + (slot >> 3));
@@ -487,7 +502,7 @@ __device__ __forceinline__ int deeper_rank(int mycnt, int lane) {
 // -- and lanes 0..7 write the empty octants.
 __device__ int small_subtree(const StepParams& p, const int* __restrict__ src, int lo, int m, int cell, int level,
                              float cx, float cy, float cz, float r, SmallTask* st, int& local_max, bool build,
-                             int base) {
+                             int base, bool zero_counts) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int nbody = p.nbody;
@@ -525,6 +540,8 @@ __device__ int small_subtree(const StepParams& p, const int* __restrict__ src, i
                 p.arrive[t.cell - nbody] = 0;
                 p.clevel[t.cell - nbody] = t.level;
             }
+            if (zero_counts && lane < 2)   // bucket counters for a pass into this tree
+                reinterpret_cast<int4*>(p.kids4 + ((size_t)(t.cell - nbody) << 3))[lane] = make_int4(0, 0, 0, 0);
         }
         // the largest child cell is pushed deepest (popped last); the others above it
         int pos = 0;
@@ -558,8 +575,8 @@ __device__ int small_subtree(const StepParams& p, const int* __restrict__ src, i
 
 // Both passes with an allocation of their own in between (the large-bucket path).
 __device__ int build_small(const StepParams& p, const int* __restrict__ src, int lo, int m, int cell, int level,
-                           float cx, float cy, float cz, float r, SmallTask* st, int& local_max) {
-    const int need = small_subtree(p, src, lo, m, cell, level, cx, cy, cz, r, st, local_max, false, 0);
+                           float cx, float cy, float cz, float r, SmallTask* st, int& local_max, bool zero_counts) {
+    const int need = small_subtree(p, src, lo, m, cell, level, cx, cy, cz, r, st, local_max, false, 0, false);
     if (need < 0) return -1;
     int base = 0;
     if (need > 0) {
@@ -570,10 +587,10 @@ __device__ int build_small(const StepParams& p, const int* __restrict__ src, int
             return -1;
         }
     }
-    return small_subtree(p, src, lo, m, cell, level, cx, cy, cz, r, st, local_max, true, base);
+    return small_subtree(p, src, lo, m, cell, level, cx, cy, cz, r, st, local_max, true, base, zero_counts);
 }
 
-__global__ void __launch_bounds__(32 * kBucketWarps) bucket_build_kernel(StepParams p) {
+__global__ void __launch_bounds__(32 * kBucketWarps) bucket_build_kernel(StepParams p, bool zero_counts) {
     __shared__ SmallTask small_all[kBucketWarps][kSmallStack];
     if (load_status(p.st)) return;
     BucketTask* stack = static_cast<BucketTask*>(p.bstack) +
@@ -619,7 +636,7 @@ __global__ void __launch_bounds__(32 * kBucketWarps) bucket_build_kernel(StepPar
                                             __fadd_rn(__fsub_rn(g.x, h0), (j & 1) ? g.w : 0.0f),
                                             __fadd_rn(__fsub_rn(g.y, h0), (j & 2) ? g.w : 0.0f),
                                             __fadd_rn(__fsub_rn(g.z, h0), (j & 4) ? g.w : 0.0f), h0, sstack,
-                                            local_max, false, 0);
+                                            local_max, false, 0, false);
             if (cells < 0) return;
             if (lane == it) need = cells;
         }
@@ -668,7 +685,7 @@ __global__ void __launch_bounds__(32 * kBucketWarps) bucket_build_kernel(StepPar
             int root;
             if (m <= 32) {
                 root = small_subtree(p, p.bwork, start, m, -1, clev + 1, rcx, rcy, rcz, h0, sstack, local_max, true,
-                                     sub_base);
+                                     sub_base, zero_counts);
                 if (root < 0) return;
                 if (lane == 0) *slot = root;
                 continue;
@@ -690,7 +707,7 @@ __global__ void __launch_bounds__(32 * kBucketWarps) bucket_build_kernel(StepPar
                 int* dst = p.bwork + (t.buf ? 0 : nbody);
                 if (t.hi - t.lo <= 32) {                  // small enough for the register builder
                     if (build_small(p, src, t.lo, t.hi - t.lo, t.cell, t.level, t.cx, t.cy, t.cz, t.r, sstack,
-                                    local_max) < 0) {
+                                    local_max, zero_counts) < 0) {
                         ok = false;
                         break;
                     }
@@ -780,6 +797,8 @@ __global__ void __launch_bounds__(32 * kBucketWarps) bucket_build_kernel(StepPar
                     p.arrive[t.cell - nbody] = 0;
                     p.clevel[t.cell - nbody] = t.level;
                 }
+                if (zero_counts && lane < 2)
+                    reinterpret_cast<int4*>(p.kids4 + ((size_t)(t.cell - nbody) << 3))[lane] = make_int4(0, 0, 0, 0);
                 top += nc;
                 __syncwarp();
             }
@@ -982,24 +1001,40 @@ void launch_bbox(const StepParams& p, int grid, cudaStream_t s) {
     if (p.precise) bbox_kernel<true><<<grid, 256, 0, s>>>(p);
     else bbox_kernel<false><<<grid, 256, 0, s>>>(p);
 }
+// One bucketed completion: the bodies of `set` join the subtrees of the slots of the tree
+// built so far.  zero_counts: the new cells get bucket counters for a later pass.
+static void launch_bucket_pass(const StepParams& p, BuildPhase set, bool first, bool zero_counts, int sms,
+                               cudaStream_t s) {
+    const long long rest = (long long)p.nchunks * phase_bodies(set);
+    const unsigned grid_rest = (unsigned)((rest + 255) / 256);
+    bucket_locate_kernel<<<grid_rest, 256, 0, s>>>(p, set, !first);
+    // every cell of the tree so far: at most one per inserted body (1/16 of each chunk) plus
+    // the roots
+    const long long cells = (long long)p.nchunks * 16 + p.nuniv;
+    bucket_alloc_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(p);
+    bucket_scatter_kernel<<<grid_rest, 256, 0, s>>>(p, set);
+    bucket_build_kernel<<<kBucketBlocksPerSm * sms, 32 * kBucketWarps, 0, s>>>(p, zero_counts);
+}
+
 void launch_build(const StepParams& p, int phases, bool buckets, int sms, cudaStream_t s) {
+    buckets = buckets && phases != 1;
+    if (buckets && phases == 3) {
+        // one lock phase (1/256 of each chunk), then the rest of the 1/16 sample as bucket
+        // subtrees of that tree, then every other body as bucket subtrees of the sample's
+        build_kernel<<<(unsigned)((p.nchunks * (long long)phase_bodies(kThreePhases[0]) + 255) / 256), 256, 0, s>>>(
+            p, kThreePhases[0], true);
+        launch_bucket_pass(p, kThreePhases[1], true, true, sms, s);
+        launch_bucket_pass(p, kBucketBodies, false, false, sms, s);
+        return;
+    }
     const BuildPhase* sched = phases == 1 ? kOnePass : (phases == 5 ? kFivePhases : kThreePhases);
     int count = phases == 1 ? 1 : (phases == 5 ? 5 : 3);
-    buckets = buckets && phases != 1;
-    if (buckets) count -= phases == 5 ? 2 : 1;   // the lock phases insert the 1/16 sample only
+    if (buckets) count -= 2;   // five phases: the lock phases insert the 1/16 sample only
     for (int k = 0; k < count; ++k) {
         const long long bodies = (long long)p.nchunks * phase_bodies(sched[k]);
         build_kernel<<<(unsigned)((bodies + 255) / 256), 256, 0, s>>>(p, sched[k], buckets);
     }
-    if (!buckets) return;
-    const long long rest = (long long)p.nchunks * phase_bodies(kBucketBodies);
-    const unsigned grid_rest = (unsigned)((rest + 255) / 256);
-    bucket_locate_kernel<<<grid_rest, 256, 0, s>>>(p);
-    // every cell of the sampled tree: at most one per sampled body plus the roots
-    const long long cells = (long long)p.nchunks * 16 + p.nuniv;
-    bucket_alloc_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(p);
-    bucket_scatter_kernel<<<grid_rest, 256, 0, s>>>(p);
-    bucket_build_kernel<<<kBucketBlocksPerSm * sms, 32 * kBucketWarps, 0, s>>>(p);
+    if (buckets) launch_bucket_pass(p, kBucketBodies, true, false, sms, s);
 }
 
 size_t bucket_stack_bytes(int sms) {

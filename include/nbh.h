@@ -90,10 +90,12 @@ typedef struct nbh_config {
                               multiple of 8 (0: 256); trees deeper than (cap - 8) / 7 + 1
                               levels take the per-level walk */
     int32_t build_phases;  /* octree insertion launches: 1 (one pass), 3 or 5 (0: 5) */
-    int32_t build_buckets; /* 1 (or 0, the default): with 3 or 5 phases the lock phases
-                              insert a 1/16 sample of the bodies and every other body joins
-                              the subtree of the sample-tree slot it descends to, built by one
-                              warp without locks (the same tree); 2: lock insertion only */
+    int32_t build_buckets; /* 1 (or 0, the default): with 5 phases the lock phases insert a
+                              1/16 sample of the bodies and every other body joins the
+                              subtree of the sample-tree slot it descends to, built by one
+                              warp without locks (the same tree); with 3 phases one lock
+                              phase inserts 1/256 and two such passes add the rest of the
+                              sample, then the other bodies; 2: lock insertion only */
     int32_t reserved[4];
 } nbh_config;
 

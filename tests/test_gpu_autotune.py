@@ -126,3 +126,46 @@ def test_bucketed_build_when_the_sample_misses_a_cluster():
     for k in KEYS:
         np.testing.assert_array_equal(out[1][1][k], out[2][1][k])
     assert out[1][2]["max_depth"] == out[2][2]["max_depth"] and out[1][2]["status"] == 0
+
+
+def test_close_pairs_inside_the_sample_make_long_chains():
+    """Close pairs whose both bodies fall in the build's 1/16 sample (offsets o and o + 16
+    of a chunk, o on the sample lattice): the sample tree then holds long chains of cells
+    with one cell child (~17 levels per pair), many more cells than sampled bodies.  Every
+    build schedule -- one lock pass, five lock phases, five phases with the bucketed
+    completion, one lock phase with two bucketed passes -- gives the same tree and forces,
+    with every body reachable once from the root."""
+    n = 16 * 4096
+    r = np.random.default_rng(87)
+    pos = r.uniform(-1, 1, (n, 3)).astype(np.float32)
+    for c in range(n // 256):
+        rot = (7 * c) & 15
+        for k in range(8):
+            a = c * 256 + rot + 32 * k
+            pos[a + 16] = pos[a] + np.float32(1e-5) * np.array([1.0, 0.7, 0.3], np.float32)
+    zero = np.zeros(n, np.float32)
+    m = np.full(n, 1.0 / n, np.float32)
+    arrs = (pos[:, 0].copy(), pos[:, 1].copy(), pos[:, 2].copy(), zero, zero, zero, m)
+    out = {}
+    for phases, buckets in ((5, 2), (1, 2), (5, 1), (3, 1)):
+        g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, build_phases=phases, build_buckets=buckets)
+        g.load(*arrs)
+        g.step(1)
+        t = g.tree()
+        ch = t["child"]
+        front, seen = np.array([t["nnodes"]]), []
+        while front.size:
+            kids = ch[front - n].ravel()
+            seen.append(kids[(kids >= 0) & (kids < n)])
+            front = kids[kids >= n]
+        seen = np.concatenate(seen)
+        assert seen.size == n and np.unique(seen).size == n, (phases, buckets)
+        st = g.stats()
+        assert st["status"] == 0 and st["cells"] > n // 2, (phases, buckets, st["cells"])
+        out[(phases, buckets)] = (t["sorted"], g.read())
+        g.close()
+    ref = out[(5, 2)]
+    for key, (srt, state) in out.items():
+        np.testing.assert_array_equal(srt, ref[0], err_msg=str(key))
+        for k in KEYS:
+            np.testing.assert_array_equal(state[k], ref[1][k], err_msg="%s %s" % (key, k))
