@@ -43,12 +43,15 @@ DEFAULT_VOTE = 64                   # libnbh's default vote width (nbh_config_de
 def graph_launches(build_phases=5, build_buckets=1):
     """Kernels in one fixed-angle step graph: bbox, the build's launches, link, summarize,
     sort, force, the work-item order of the next force launch, integrate.  The build is
-    `build_phases` lock phases, or with the bucketed completion the phases up to the 1/16
-    sample (2 of 3, 3 of 5) plus locate, alloc, scatter and subtree build."""
+    `build_phases` lock phases, or with the bucketed completion: five phases -> the three
+    lock phases of the 1/16 sample and one bucketed pass (locate, alloc, scatter, subtree
+    build); three phases -> one lock phase (1/256) and two bucketed passes."""
     if build_phases == 1 or build_buckets == 2:
         build = build_phases
+    elif build_phases == 5:
+        build = 3 + 4
     else:
-        build = (3 if build_phases == 5 else 2) + 4
+        build = 1 + 2 * 4
     return 7 + build
 FLOPS_PER_INTERACTION = 20          # 3 sub, 3 fma (d^2+eps^2), rsqrt, 3 mul, 3 fma, ~7 more
 HBM_FALLBACK_GBS = 6800.0

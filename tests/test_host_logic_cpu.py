@@ -34,7 +34,7 @@ def test_graph_launch_count_follows_the_build_schedule():
     import bench
     # bbox, link, summarize, sort, force, item order, integrate = 7, plus the build
     assert bench.graph_launches() == 7 + 3 + 4                 # five phases, bucketed
-    assert bench.graph_launches(3, 1) == 7 + 2 + 4
+    assert bench.graph_launches(3, 1) == 7 + 1 + 2 * 4              # one lock phase, two bucketed passes
     assert bench.graph_launches(5, 2) == 7 + 5
     assert bench.graph_launches(1, 2) == 7 + 1
     assert bench.graph_launches(1, 1) == 7 + 1                 # one pass has no bucketed completion
