@@ -162,7 +162,8 @@ def _reachable_bodies(t, n, roots=None):
 def test_rebuilds_under_contention_hold_every_body_and_repeat():
     """1M-body Plummer sphere with dt = 0: every step rebuilds the same octree from the same
     positions.  Under every build schedule (one lock pass: all bodies contend at once; five
-    lock phases; five phases with the bucketed completion) each rebuild reaches every body
+    lock phases; five phases with the bucketed completion; one lock phase with two bucketed
+    passes) each rebuild reaches every body
     exactly once from the root, counts them all, and gives the same depth-first order and
     the same accelerations, bit for bit, as every other rebuild and schedule.  (Summarize
     used to decide from a cell's slots while the cell's own compaction rewrote them; in up to
@@ -170,7 +171,7 @@ def test_rebuilds_under_contention_hold_every_body_and_repeat():
     n = 1 << 20
     arrs = plummer(n, seed=1)
     ref = None
-    for phases, buckets, steps in ((1, 2, 12), (5, 2, 5), (5, 1, 5)):
+    for phases, buckets, steps in ((1, 2, 12), (5, 2, 5), (5, 1, 5), (3, 1, 5)):
         g = gpu_sim(theta=0.5, eps=0.05, dt=0.0, vote_width=64, build_phases=phases, build_buckets=buckets)
         g.load(*arrs)
         for s in range(steps):
@@ -426,8 +427,9 @@ def test_step_io_equals_write_step_read():
 
 def test_batch_rebuilds_under_contention_hold_every_body_and_repeat():
     """A batch of 192 Plummer universes (1 to 40,000 bodies, 625,654 in all) with dt = 0, built in
-    one lock pass (every universe's bodies contend in its top levels at once) and with the
-    default schedule: every rebuild reaches every body once from its own universe's root,
+    one lock pass (every universe's bodies contend in its top levels at once), with the
+    default schedule and with the two-pass bucketed one: every rebuild reaches every body
+    once from its own universe's root,
     and repeats the depth-first order and the accelerations bit for bit."""
     from nbh import universe as U
     rng = np.random.default_rng(11)
@@ -438,7 +440,7 @@ def test_batch_rebuilds_under_contention_hold_every_body_and_repeat():
     n = int(counts.sum())
     off = np.concatenate([[0], np.cumsum(counts)])
     ref = None
-    for phases, buckets in ((1, 2), (5, 1)):
+    for phases, buckets in ((1, 2), (5, 1), (3, 1)):
         g = gpu_sim(theta=0.5, eps=0.05, dt=0.0, vote_width=64, build_phases=phases, build_buckets=buckets)
         g.load_batch(counts, *cat)
         for s in range(4):
