@@ -846,11 +846,25 @@ int nbh_write(nbh_sim* sim, const float* x, const float* y, const float* z, cons
     return NBH_OK;
 }
 
+namespace {
+int step_io(nbh_sim* sim, int32_t nsteps, const nbh_host_state* in, const nbh_host_state* out);
+}  // namespace
+
 int nbh_step_io(nbh_sim* sim, int32_t nsteps, const nbh_host_state* in, const nbh_host_state* out) {
     if (!sim) return NBH_ERR_INVALID;
     if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_step_io before nbh_load");
     if (nsteps < 0) return fail(sim, NBH_ERR_INVALID, "nsteps < 0");
     CK(cudaSetDevice(sim->device));
+    int e = step_io(sim, nsteps, in, out);
+    // on an error after the side copies were queued, they may still be reading the caller's
+    // arrays: wait for them before handing the arrays back
+    if (e && sim->io_stream) cudaStreamSynchronize(sim->io_stream);
+    return e;
+}
+
+namespace {
+
+int step_io(nbh_sim* sim, int32_t nsteps, const nbh_host_state* in, const nbh_host_state* out) {
     int e;
     int rest = nsteps;
     if (in) {
@@ -895,6 +909,8 @@ int nbh_step_io(nbh_sim* sim, int32_t nsteps, const nbh_host_state* in, const nb
     CK(cudaStreamSynchronize(sim->stream));
     return finish_steps(sim, nsteps);
 }
+
+}  // namespace
 
 int nbh_get_stats(nbh_sim* sim, nbh_stats* out) {
     if (!sim || !out) return NBH_ERR_INVALID;
