@@ -116,13 +116,15 @@ def test_fma_mode_ten_steps_positions():
         assert np.abs(gs[k] - os_[k]).max() <= 1e-5 * scale, k
 
 
-def test_tree_matches_oracle_and_invariants():
+@pytest.mark.parametrize("phases,buckets", [(5, 1), (3, 1), (5, 2), (1, 2)],
+                         ids=["five-bucketed", "two-pass-bucketed", "five-lock", "one-pass"])
+def test_tree_matches_oracle_and_invariants(phases, buckets):
     """Same octree as the oracle (slot by slot), every body in exactly one slot, body
     counts add up, root mass = total mass, centres of mass equal the oracle's bit for bit
-    (same summation order)."""
+    (same summation order) -- under every build schedule."""
     n = 20000
     arrs = plummer(n, seed=9)
-    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=32)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=32, build_phases=phases, build_buckets=buckets)
     g.load(*arrs)
     g.step()
     o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=32, fma=True)
