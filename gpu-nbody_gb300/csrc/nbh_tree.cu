@@ -455,12 +455,14 @@ __global__ void __launch_bounds__(256) bucket_scatter_kernel(StepParams p, Build
 }
 
 // (4) build: one warp per bucket builds the bucket's subtree by splitting its bodies by
-// octant, level by level (depth first over a shared-memory task stack), writing each new
-// cell's 8 slots once with their final values, then stores the subtree's root into the
-// slot.  Subtrees of at most 32 bodies are built in registers (one body per lane, octant
-// splits by ballots over lane masks): a counting pass sizes the subtree so one atomic takes
-// all its cells, then the writing pass hands them out parents first.  Larger buckets split
-// through the two halves of bwork until a part has at most 32 bodies.
+// octant, level by level (depth first over a task stack), writing each new cell's 8 slots
+// once with their final values, then stores the subtree's root into the slot.  Subtrees of
+// at most 32 bodies are built in registers (one body per lane, octants grouped by
+// match_any).  A warp takes kBucketChunk buckets per work-counter atomic; a counting pass
+// sizes the register subtrees of the whole chunk so that one allocator atomic takes all
+// their cells, then the writing pass hands each subtree its share, parents first.  (Both
+// counters sit on one L2 slice: one atomic per bucket each was the kernel's limit.)  Larger
+// buckets split through the two halves of bwork until a part has at most 32 bodies.
 struct BucketTask {
     int cell, level, lo, hi, buf;
     float cx, cy, cz, r;       // centre and half-width of `cell`
