@@ -855,10 +855,17 @@ int nbh_step_io(nbh_sim* sim, int32_t nsteps, const nbh_host_state* in, const nb
     if (!sim->loaded) return fail(sim, NBH_ERR_STATE, "nbh_step_io before nbh_load");
     if (nsteps < 0) return fail(sim, NBH_ERR_INVALID, "nsteps < 0");
     CK(cudaSetDevice(sim->device));
+    const auto steps0 = sim->steps;
     int e = step_io(sim, nsteps, in, out);
-    // on an error after the side copies were queued, they may still be reading the caller's
-    // arrays: wait for them before handing the arrays back
-    if (e && sim->io_stream) cudaStreamSynchronize(sim->io_stream);
+    if (e) {
+        // On an error after work was queued, the side copies (io_stream) and the packing and
+        // unpacking kernels (the sim's stream) may still read or write the caller's arrays:
+        // wait for both before handing the arrays back.  The steps count only a call that
+        // succeeded as a whole.
+        if (sim->io_stream) cudaStreamSynchronize(sim->io_stream);
+        cudaStreamSynchronize(sim->stream);
+        sim->steps = steps0;
+    }
     return e;
 }
 
@@ -1295,8 +1302,8 @@ int nbh_direct_f64_static(nbh_sim* sim, int32_t nidx, const int32_t* idx, double
     if (nidx == 0) return NBH_OK;
     for (int t = 0; t < nidx; ++t)
         if (idx[t] < 0 || idx[t] >= sim->nbody) return fail(sim, NBH_ERR_INVALID, "body index out of range");
-    CK(cudaSetDevice(sim->device));
     if (sim->device < 0 || sim->device >= kMaxDevices) return fail(sim, NBH_ERR_INVALID, "device ordinal too large");
+    CK(cudaSetDevice(sim->device));
     StaticDirectScratch* sc = nullptr;
     CK(direct_scratch_for(sim->device, &sc));
     cudaStream_t s = sim->stream;

@@ -351,9 +351,12 @@ int nbh_mlp_forward(int32_t device, const float* params, const float* X, int32_t
  * NBH_DIRECT_STATIC_MAX bodies per call; larger lists are rejected with NBH_ERR_INVALID.
  * That array is reserved on every GPU that loads the library until the process exits.  The
  * first call on a device looks the array's device address up (cudaGetSymbolAddress, with the
- * sim's device current), so make that first call before any stream capture.  All calls share
- * the array: it is cleared at the start of every call, and calls that overlap on the GPU (two
- * sims on different streams at the same time) race on it.  No counterpart in the reference. */
+ * sim's device current), so make that first call before any stream capture.  The address is
+ * kept for the life of the process: the library never resets a device, and a host
+ * application that calls cudaDeviceReset must not call this entry point afterwards.  All
+ * calls share the array: it is cleared at the start of every call, and calls that overlap on
+ * the GPU (two sims on different streams at the same time) race on it.  No counterpart in the
+ * reference. */
 #define NBH_DIRECT_STATIC_MAX 65536
 int nbh_direct_f64_static(nbh_sim* sim, int32_t nidx, const int32_t* idx,
                           double* ax, double* ay, double* az);

@@ -184,12 +184,17 @@ def test_universe_reader_rejects_garbage(tmp_path):
         U.SerializedUniverseGenerator(p)
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/universes/sphericaluniverse1.universe"),
+def _reference_fixture(name):
+    import build as B                       # oracle/build.py: NBH_REFERENCE_ROOT or the default
+    return os.path.join(B.REFERENCE_ROOT, "universes", name)
+
+
+@pytest.mark.skipif(not os.path.exists(_reference_fixture("sphericaluniverse1.universe")),
                     reason="reference fixtures not mounted")
 def test_reads_reference_universe_fixture():
     """universes/sphericaluniverse1.universe: 32768 bodies on the unit sphere at rest,
     masses 1/32768 (written by UniverseSerializer.java)."""
-    g = U.SerializedUniverseGenerator("/root/reference/universes/sphericaluniverse1.universe")
+    g = U.SerializedUniverseGenerator(_reference_fixture("sphericaluniverse1.universe"))
     x, y, z, vx, vy, vz, m = g.arrays(32768)
     r = np.sqrt(x.astype(np.float64) ** 2 + y ** 2 + z ** 2)
     np.testing.assert_allclose(r, 1.0, rtol=1e-5)

@@ -49,3 +49,29 @@ def test_static_scratch_rejects_oversized_lists_and_recovers():
     want = sim.direct_f64(idx)
     for g, w in zip(got, want):
         np.testing.assert_allclose(g, w, rtol=1e-10, atol=1e-13)
+
+
+def test_static_scratch_full_array_and_batched_universes():
+    """A list of exactly NBH_DIRECT_STATIC_MAX targets fills the whole array; a batch of
+    uneven universes (one of them a single body) makes each target find its own universe's
+    body range on the device, which must agree with the allocating entry point's ranges."""
+    from nbh import _lib as L
+    rng = np.random.default_rng(8)
+    counts = np.array([1, 700, 40000, 5, 31000, 1], np.int32)
+    parts = [plummer(int(c), seed=30 + u) for u, c in enumerate(counts)]
+    arrs = [np.concatenate([p[k] for p in parts]) for k in range(7)]
+    n = int(counts.sum())
+    sim = gpu_sim(theta=0.5, eps=0.05, dt=0.01)
+    sim.load_batch(counts, *arrs)
+    sim.step(1)
+    for idx in (np.sort(rng.choice(n, L.NBH_DIRECT_STATIC_MAX, replace=False)).astype(np.int32),
+                np.array([0, 1, n - 1, 701, 40701, 40705, 71705, 71704], np.int32)):
+        code, got = _static(sim, idx)
+        assert code == L.NBH_OK, sim._L.nbh_last_error_message(sim._h)
+        want = sim.direct_f64(idx)
+        for g, w in zip(got, want):
+            np.testing.assert_allclose(g, w, rtol=1e-10, atol=1e-13)
+    # a single-body universe feels no force at all
+    code, got = _static(sim, np.array([0, n - 1], np.int32))
+    assert code == L.NBH_OK
+    assert all(np.all(g == 0.0) for g in got)
