@@ -297,15 +297,41 @@ def _config(args, nbodies=None, counts=None):
     return c
 
 
-def _step_error(sim, idx, O, np):
-    """Relative force error of the next step's accelerations against the FP64 direct sum
-    at the positions that step starts from (sampled bodies)."""
-    ref = sim.direct_f64(idx)
-    sim.step(1)
-    st = sim.read()
-    e = O.rel_force_error(st["ax"][idx], st["ay"][idx], st["az"][idx], *ref)
-    return {"median": float(np.median(e)), "p99": float(np.percentile(e, 99)), "samples": int(idx.size),
-            "vs": "FP64 direct sum", "interactions": int(sim.stats()["interactions"])}
+def _cycle_error(sim, idx, steps, O, np):
+    """Relative force error against the FP64 direct sum over `steps` consecutive steps: at
+    each step, the accelerations of the sampled bodies `idx` against the direct sum at the
+    positions that step starts from.  With `steps` = the learned model's evaluation
+    interval every phase of its cycle is measured once.  p99 and median per step, their
+    mean and the worst step's p99, and the mean interactions per step."""
+    p99, med, inter = [], [], []
+    for _ in range(steps):
+        ref = sim.direct_f64(idx)
+        sim.step(1)
+        st = sim.read()
+        e = O.rel_force_error(st["ax"][idx], st["ay"][idx], st["az"][idx], *ref)
+        p99.append(float(np.percentile(e, 99)))
+        med.append(float(np.median(e)))
+        inter.append(int(sim.stats()["interactions"]))
+    return {"p99": float(np.mean(p99)), "p99_max": float(np.max(p99)), "median": float(np.mean(med)),
+            "p99_per_step": p99, "steps": steps, "samples": int(idx.size), "vs": "FP64 direct sum",
+            "interactions": float(np.mean(inter))}
+
+
+def _stage_cycle(sim, steps, flush_l2, stream, torch):
+    """Per-stage device times of `steps` consecutive stage-timed steps (L2 flushed before
+    each): the mean of each stage and, per step, the force and learned-angle stages."""
+    keys = ("ms_bbox", "ms_build", "ms_summarize", "ms_sort", "ms_theta", "ms_force", "ms_integrate", "ms_step")
+    acc = {k: 0.0 for k in keys}
+    force, theta = [], []
+    for _ in range(steps):
+        flush_l2(stream)
+        sim.step(1)
+        s2 = sim.stats()
+        for k in keys:
+            acc[k] += s2[k] / steps
+        force.append(s2["ms_force"])
+        theta.append(s2["ms_theta"])
+    return acc, force, theta, sim.stats()
 
 
 def _timed_steps(sim, steps, flush_l2, stream, torch, dev):
@@ -417,7 +443,12 @@ def main():
     tune = None if (args.no_autotune or args.profile_only) else sim.autotune(vote=args.tune_vote)
     if tune is not None:
         args.vote_width = int(tune["vote_width"])
-    force_error = None if args.profile_only else _step_error(sim, idx, O, np)
+    # the error of both arms over the same steps: one full evaluation cycle of the learned
+    # model (every phase of it once), from the same step index
+    model_path = LR.default_model_path()
+    model = LR.load_model(model_path) if (not args.no_learned and os.path.exists(model_path)) else None
+    cycle = max(8, int(model.get("every", 1))) if model is not None else 8
+    force_error = None if args.profile_only else _cycle_error(sim, idx, cycle, O, np)
     clocks = ClockSampler(local) if rank == 0 else None
     if clocks:
         clocks.start()
@@ -444,15 +475,8 @@ def main():
     ts = new_sim(stage_timing=True, **geometry)
     ts.step(2)
     tstream = torch.cuda.ExternalStream(ts.stream, device=dev)
-    acc = {k: 0.0 for k in ("ms_bbox", "ms_build", "ms_summarize", "ms_sort", "ms_force", "ms_integrate", "ms_step")}
-    reps = 5
-    for _ in range(reps):
-        with torch.cuda.stream(tstream):
-            flush.zero_()
-        ts.step(1)
-        s2 = ts.stats()
-        for k in acc:
-            acc[k] += s2[k] / reps
+    acc, _, _, s2 = _stage_cycle(ts, 5, flush_l2, tstream, torch)
+    acc.pop("ms_theta")
     cells = int(s2["cells"])
     inter_ts = int(s2["interactions"])
     ts.close()
@@ -525,32 +549,47 @@ def main():
 
     # ---- learned per-body theta: same protocol ----------------------------------------
     learned = None
-    model_path = LR.default_model_path()
-    if not args.no_learned and os.path.exists(model_path):
-        model = LR.load_model(model_path)
+    if model is not None:
         ls = new_sim(**geometry)
         LR.install(ls, model)
         lstream = torch.cuda.ExternalStream(ls.stream, device=dev)
         for _ in range(args.warmup):
             flush_l2(lstream)
             ls.step(1)
-        lerr = _step_error(ls, idx, O, np)
-        lstep_ms, lst = _timed_steps(ls, args.steps, flush_l2, lstream, torch, dev)
+        # the same step indices as the plain arm's error, the same sampled bodies
+        lerr = _cycle_error(ls, idx, cycle, O, np)
+        # timed steps: a whole number of model cycles, so every phase weighs the same
+        lsteps = max(cycle, (args.steps + cycle - 1) // cycle * cycle)
+        lstep_ms, lst = _timed_steps(ls, lsteps, flush_l2, lstream, torch, dev)
         lms = max_over_ranks(sum(lstep_ms) / len(lstep_ms))
         th = LR.read_theta(ls)
+        ls.close()
+        # the learned step's own stages over one cycle: features + inference (theta), the
+        # walks with and without the error-bound recording
+        lt = new_sim(stage_timing=True, **geometry)
+        LR.install(lt, model)
+        lt.step(args.warmup)
+        ltstream = torch.cuda.ExternalStream(lt.stream, device=dev)
+        lacc, lforce, ltheta, _ = _stage_cycle(lt, cycle, flush_l2, ltstream, torch)
+        lt.close()
         learned = {
             "ms_per_step": lms / (world if args.workload != "ensemble" else 1), "speedup_vs_plain": ms / lms,
+            "timed_steps": lsteps,
             "force_error": lerr, "p99_vs_plain": lerr["p99"] / force_error["p99"],
-            "equal_or_lower_p99": bool(lerr["p99"] <= force_error["p99"]),
-            "interactions_per_step": int(lst["interactions"]),
-            "interaction_ratio_vs_plain": interactions / max(1, int(lst["interactions"])),
+            "p99_max_vs_plain": lerr["p99_max"] / force_error["p99_max"],
+            "equal_or_lower_p99": bool(lerr["p99"] <= force_error["p99"]
+                                       and lerr["p99_max"] <= force_error["p99_max"]),
+            "stage_ms": {k[3:]: v for k, v in lacc.items()},
+            "theta_ms_per_step": lacc["ms_theta"], "theta_share_of_step": lacc["ms_theta"] / lacc["ms_step"],
+            "theta_ms_per_step_list": ltheta, "force_ms_per_step_list": lforce,
+            "interactions_per_step": lerr["interactions"],
+            "interaction_ratio_vs_plain": force_error["interactions"] / max(1.0, lerr["interactions"]),
             "theta_mean": float(th.mean()), "theta_p10": float(np.percentile(th, 10)),
             "theta_p90": float(np.percentile(th, 90)),
             "model": os.path.relpath(model_path, ROOT),
-            "gint_per_s": int(lst["interactions"]) * (world if args.workload != "ensemble" else 1)
+            "gint_per_s": lerr["interactions"] * (world if args.workload != "ensemble" else 1)
                           / (lms * 1e-3) / 1e9,
         }
-        ls.close()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -69,11 +69,11 @@ struct nbh_sim {
     cudaGraphExec_t exec = nullptr;
     // host mirrors
     DevState* h_state = nullptr;   // pinned
-    cudaEvent_t ev[7] = {};
+    cudaEvent_t ev[8] = {};   // stage boundaries; ev[7]: end of sort, start of the theta stage
     // nbh_step_io: velocities and accelerations go up on io_stream while the tree stages run
     cudaStream_t io_stream = nullptr;
     cudaEvent_t io_start = nullptr, io_ready = nullptr;
-    float stage_ms[7] = {};
+    float stage_ms[8] = {};
     bool loaded = false;
     int64_t steps = 0;
     int last_err = NBH_OK;
@@ -225,6 +225,7 @@ void enqueue_step(nbh_sim* sim, bool timed, cudaEvent_t vel_acc_ready = nullptr,
     launch_summarize(p, ref, sim->grid_sum, s);
     if (timed) cudaEventRecord(sim->ev[3], s);
     launch_sort(p, sim->grid_sort, s);
+    if (timed) cudaEventRecord(sim->ev[7], s);
     if (vel_acc_ready) {
         cudaStreamWaitEvent(s, vel_acc_ready, 0);
         launch_pack(sim->nbody, sim->staging, staged_mask, sim->node4, sim->vel, sim->acc,
@@ -737,6 +738,9 @@ int finish_steps(nbh_sim* sim, int32_t nsteps) {
     if (sim->cfg.stage_timing && nsteps > 0) {
         for (int k = 0; k < 6; ++k) cudaEventElapsedTime(&sim->stage_ms[k], sim->ev[k], sim->ev[k + 1]);
         cudaEventElapsedTime(&sim->stage_ms[6], sim->ev[0], sim->ev[6]);
+        // sort ends at ev[7]; ev[7] -> ev[4] is the learned-angle stage (empty without a model)
+        cudaEventElapsedTime(&sim->stage_ms[3], sim->ev[3], sim->ev[7]);
+        cudaEventElapsedTime(&sim->stage_ms[7], sim->ev[7], sim->ev[4]);
     }
     const int status = sim->h_state->status;
     if (status != NBH_OK) {
@@ -946,6 +950,7 @@ int nbh_get_stats(nbh_sim* sim, nbh_stats* out) {
     out->ms_force = sim->stage_ms[4];
     out->ms_integrate = sim->stage_ms[5];
     out->ms_step = sim->stage_ms[6];
+    out->ms_theta = sim->stage_ms[7];
     return NBH_OK;
 }
 

@@ -57,7 +57,7 @@ class NbhStats(C.Structure):
         ("lock_waits", C.c_int32), ("cas_misses", C.c_int32),
         ("ms_bbox", C.c_float), ("ms_build", C.c_float), ("ms_summarize", C.c_float),
         ("ms_sort", C.c_float), ("ms_force", C.c_float), ("ms_integrate", C.c_float),
-        ("ms_step", C.c_float), ("reserved", C.c_float * 8),
+        ("ms_step", C.c_float), ("ms_theta", C.c_float), ("reserved", C.c_float * 7),
     ]
 
 

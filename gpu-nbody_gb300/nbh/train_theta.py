@@ -32,13 +32,19 @@ from nbh import learned as LR  # noqa: E402
 from nbh import universe as U  # noqa: E402
 
 
-def evaluate(arrs, model, theta=0.5, eps=0.05, dt=0.01, nsample=4096, warm=3, cycle=4, timed=16, seed=17,
+def evaluate(arrs, model, theta=0.5, eps=0.05, dt=0.01, nsample=4096, warm=3, cycle=None, timed=16, seed=17,
              device=0, every=None):
     """Fixed theta (plain) against the learned angle (if model) from the same initial
     state, through the production step: after `warm` steps, the relative force error
     against FP64 on `nsample` bodies at each of `cycle` consecutive steps (p99 mean and
     max over the steps, median), the mean interactions per step, and ms/step over
-    `timed` further steps (host clock around synchronous steps)."""
+    `timed` further steps (host clock around synchronous steps).  `cycle` defaults to one
+    whole evaluation cycle of the model (its interval, at least 8 steps), so that every
+    phase of the cycle is measured once and both modes over the same step indices."""
+    if cycle is None:
+        k = every if every is not None else (int(model.get("every", 1)) if model is not None else 1)
+        cycle = max(8, k)
+    timed = max(timed, cycle) // cycle * cycle
     n = arrs[0].size
     idx = np.sort(np.random.default_rng(seed).choice(n, min(nsample, n), replace=False)).astype(np.int32)
     out = {}

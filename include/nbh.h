@@ -117,7 +117,9 @@ typedef struct nbh_stats {
     int32_t cas_misses;        /* build of the last step: lock attempts that lost the race */
     /* per-stage device milliseconds of the last step (stage_timing = 1 only) */
     float   ms_bbox, ms_build, ms_summarize, ms_sort, ms_force, ms_integrate, ms_step;
-    float   reserved[8];
+    float   ms_theta;          /* learned opening angle: features + MLP inference of the last
+                                  step (0 without a model; stage_timing = 1 only) */
+    float   reserved[7];
 } nbh_stats;
 
 typedef struct nbh_sim nbh_sim;
