@@ -60,6 +60,70 @@ def test_two_ranks_shard_universes_and_reduce_over_gloo():
     assert abs(loads[0] - loads[1]) <= cost.max()
 
 
+def _ensemble(counts, seed=5):
+    from nbh import universe as U
+    parts = [U.PlummerUniverseGenerator(seed=seed * 1000 + u).arrays(int(c)) for u, c in enumerate(counts)]
+    return tuple(np.concatenate([p[k] for p in parts]) for k in range(7))
+
+
+def _step_shard(arrs, counts, steps):
+    """What one rank does with its shard, on the oracle: every universe of the shard loaded
+    and stepped on its own (bench._oracles, the per-rank CPU path); the final state of each
+    universe and the shard's interactions of the last step."""
+    import argparse
+
+    import bench
+    args = argparse.Namespace(theta=0.5, eps=0.05, dt=0.01, vote_width=64)
+    orc = bench._oracles(arrs, counts, args)
+    for o in orc:
+        assert o.step(steps) == 0
+    return [o.state() for o in orc], sum(o.interactions for o in orc)
+
+
+def _rank_step_main(rank, world, port, counts, steps, q):
+    import torch.distributed as dist
+    import bench
+    os.environ.update({"MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        mine = bench.shard_universes(counts, world, rank)
+        arrs, sub = bench.select_universes(_ensemble(counts), counts, mine)
+        states, inter = _step_shard(arrs, sub, steps)
+        job_inter = bench.reduce_sum(inter, dist)
+        q.put((rank, mine.tolist(), states, job_inter))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_ranks_step_their_shards_like_one_process():
+    """Each of two gloo ranks selects its shard of an uneven ensemble and steps it (the
+    oracle stands in for the GPU on CPU); the union of the ranks' universes equals one
+    process stepping the whole batch, universe by universe and bit for bit, and the job's
+    interaction total is the single-process total."""
+    import torch.multiprocessing as mp
+    counts = np.array([300, 33, 1500, 1, 700, 64, 65, 2000, 129, 900], np.int64)
+    steps, world = 2, 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_step_main, args=(r, world, port, counts, steps, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    res = sorted((q.get(timeout=300) for _ in range(world)), key=lambda r: r[0])
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    whole, total = _step_shard(_ensemble(counts), counts, steps)
+    seen = set()
+    for rank, mine, states, job_inter in res:
+        assert job_inter == total
+        for u, st in zip(mine, states):
+            seen.add(u)
+            for k in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az"):
+                np.testing.assert_array_equal(st[k], whole[u][k], err_msg="universe %d %s" % (u, k))
+    assert seen == set(range(counts.size))
+
+
 def test_single_process_reductions_are_identity():
     import bench
     assert bench.reduce_max(3.5) == 3.5 and bench.reduce_sum(7) == 7
