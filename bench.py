@@ -291,7 +291,8 @@ def _config(args, nbodies=None, counts=None):
     c = {"workload": "%s-%d" % (args.workload, args.n), "n_bodies": nbodies or args.n,
          "distribution": w["what"], "theta": args.theta, "eps": args.eps, "dt": args.dt, "G": 1.0,
          "vote_width": args.vote_width, "precise": w["precise"],
-         "l2": "flushed before every timed step (256 MiB write)", "parallelism": "replicas"}
+         "l2": "flushed before every timed step (256 MiB write)", "parallelism": "replicas",
+         "error_samples": getattr(args, "error_samples", None)}
     if counts is not None:
         c.update({"universes": len(counts), "min_universe": int(min(counts)), "max_universe": int(max(counts))})
     return c
@@ -303,18 +304,31 @@ def _cycle_error(sim, idx, steps, O, np):
     positions that step starts from.  With `steps` = the learned model's evaluation
     interval every phase of its cycle is measured once.  p99 and median per step, their
     mean and the worst step's p99, and the mean interactions per step."""
-    p99, med, inter = [], [], []
+    p99, med, inter, errs = [], [], [], []
     for _ in range(steps):
         ref = sim.direct_f64(idx)
         sim.step(1)
         st = sim.read()
         e = O.rel_force_error(st["ax"][idx], st["ay"][idx], st["az"][idx], *ref)
+        errs.append(e)
         p99.append(float(np.percentile(e, 99)))
         med.append(float(np.median(e)))
         inter.append(int(sim.stats()["interactions"]))
     return {"p99": float(np.mean(p99)), "p99_max": float(np.max(p99)), "median": float(np.mean(med)),
             "p99_per_step": p99, "steps": steps, "samples": int(idx.size), "vs": "FP64 direct sum",
-            "interactions": float(np.mean(inter))}
+            "interactions": float(np.mean(inter)), "_errors": np.stack(errs)}
+
+
+def _p99_ratio_interval(el, ep, np, reps=200, seed=5):
+    """Paired bootstrap over the sampled bodies (the same bodies in both arms, every step):
+    the 2.5 and 97.5 percentiles of mean-over-steps p99(learned) / p99(plain)."""
+    rng = np.random.default_rng(seed)
+    n = el.shape[1]
+    r = []
+    for _ in range(reps):
+        b = rng.integers(0, n, n)
+        r.append(np.percentile(el[:, b], 99, axis=1).mean() / np.percentile(ep[:, b], 99, axis=1).mean())
+    return [float(np.percentile(r, 2.5)), float(np.percentile(r, 97.5))]
 
 
 def _stage_cycle(sim, steps, flush_l2, stream, torch):
@@ -372,9 +386,14 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch geometry")
     ap.add_argument("--tune-vote", action="store_true",
                     help="let the autotuner pick the vote width too (changes the interaction set)")
-    ap.add_argument("--error-samples", type=int, default=4096)
+    ap.add_argument("--error-samples", type=int, default=16384,
+                    help="bodies sampled for the FP64 error (the same bodies in both arms, every step)")
     ap.add_argument("--profile-only", action="store_true",
                     help="load, warm up and run the timed steps only (for ncu captures)")
+    ap.add_argument("--force-threads", type=int, default=0,
+                    help="force launch geometry of a --profile-only run (0: the library default)")
+    ap.add_argument("--stack-cap", type=int, default=0,
+                    help="stack entries per vote group of a --profile-only run (0: the library default)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
@@ -432,7 +451,7 @@ def main():
         return reduce_max(x, dist, dev)
 
     # ---- plain fixed theta: warm-up, error of one step, timed steps ---------------------
-    sim = new_sim()
+    sim = new_sim(**({"force_threads": args.force_threads, "stack_cap": args.stack_cap} if args.profile_only else {}))
     args.vote_width = int(sim.config.vote_width)
     stream = torch.cuda.ExternalStream(sim.stream, device=dev)
     for _ in range(args.warmup):
@@ -577,6 +596,7 @@ def main():
             "timed_steps": lsteps,
             "force_error": lerr, "p99_vs_plain": lerr["p99"] / force_error["p99"],
             "p99_max_vs_plain": lerr["p99_max"] / force_error["p99_max"],
+            "p99_vs_plain_95ci": _p99_ratio_interval(lerr.pop("_errors"), force_error["_errors"], np),
             "equal_or_lower_p99": bool(lerr["p99"] <= force_error["p99"]
                                        and lerr["p99_max"] <= force_error["p99_max"]),
             "stage_ms": {k[3:]: v for k, v in lacc.items()},
@@ -607,6 +627,8 @@ def main():
     replicas = args.workload != "ensemble"
     div = world if replicas else 1
     job_inter = interactions * world if replicas else reduce_sum(interactions, dist, dev)
+    if force_error is not None:
+        force_error.pop("_errors", None)
     if rank == 0:
         line = {
             "metric": METRIC, "value": ms / div, "unit": "ms/step", "n_gpus": world,

@@ -10,9 +10,11 @@ force at the angle grid on sampled bodies and measures the error against the FP6
 sum.  Candidate models are fitted for several error budgets tau (fractions of the fixed
 theta = 0.5 p99 error) and loss quantiles, then validated on a third seed through the
 production step path (features and BF16 inference inside the step, the model evaluated
-every 4 or 8 steps), each with several floors of the predicted angle; of the candidates
-whose p99 error, averaged and at its worst over one evaluation cycle of steps, does not
-exceed the fixed-theta p99 over the same steps, the fastest is kept.
+every 8 steps), each with several floors of the predicted angle, on three held-out
+spheres (16,384 sampled bodies each); of the candidates whose p99 error, averaged over one
+evaluation cycle of steps and over the spheres, stays within 0.98 of the fixed-theta p99
+over the same steps (and within 1.05 on every sphere), and whose worst step does not exceed
+fixed theta's worst on average, the fastest is kept.
 """
 from __future__ import annotations
 
@@ -32,7 +34,7 @@ from nbh import learned as LR  # noqa: E402
 from nbh import universe as U  # noqa: E402
 
 
-def evaluate(arrs, model, theta=0.5, eps=0.05, dt=0.01, nsample=4096, warm=3, cycle=None, timed=16, seed=17,
+def evaluate(arrs, model, theta=0.5, eps=0.05, dt=0.01, nsample=16384, warm=3, cycle=None, timed=16, seed=17,
              device=0, every=None):
     """Fixed theta (plain) against the learned angle (if model) from the same initial
     state, through the production step: after `warm` steps, the relative force error
@@ -111,8 +113,17 @@ def study(n=1 << 20, seed=2024, grid=(0.4, 0.45, 0.5, 0.55, 0.6, 0.7, 0.8, 0.9, 
     return out
 
 
-FLOORS = (0.35, 0.4, 0.45, 0.5)
-EVERY = (4, 8, 16)        # steps between evaluations of the model
+FLOORS = (0.36, 0.4)
+EVERY = (8,)              # steps between evaluations of the model
+TAU_FRACS = (0.5, 0.55, 0.6, 0.65)
+QUANTILES = (0.1,)
+INIT_SEEDS = (0, 1)       # initial weights of the network
+VAL_SEEDS = (103, 104, 105)   # held-out Plummer spheres of the selection
+# the p99 of one realisation moves by several per cent from sphere to sphere at the same
+# settings: a candidate's p99 ratio, averaged over the held-out spheres, must stay within
+# P99_MARGIN of fixed theta's, and on no single sphere above P99_WORST
+P99_MARGIN = 0.98
+P99_WORST = 1.05
 
 
 def main():
@@ -120,6 +131,8 @@ def main():
     ap.add_argument("--n", type=int, default=1 << 20)
     ap.add_argument("--samples", type=int, default=6144)
     ap.add_argument("--out", default=LR.default_model_path())
+    ap.add_argument("--previous", default=LR.default_model_path(),
+                    help="a model that competes in the selection with its floor and interval re-searched")
     ap.add_argument("--iters", type=int, default=1500)
     ap.add_argument("--group", type=int, default=0, help="1: each vote group walks with its smallest angle")
     ap.add_argument("--study", action="store_true", help="measure the ceiling of a per-body angle and exit")
@@ -161,35 +174,59 @@ def main():
                 print("snapshot %s seed %d part %d: p99 at theta 0.5 = %.3e, interactions %s"
                       % (name, seed, k, np.percentile(E[1], 99), I.tolist()), flush=True)
     p99_plain = float(np.median(p99s))
-    val = U.PlummerUniverseGenerator(seed=103).arrays(args.n)
-    base = evaluate(val, None)["plain"]
-    print("validation plain:", base, flush=True)
+    vals = [U.PlummerUniverseGenerator(seed=sd).arrays(args.n) for sd in VAL_SEEDS]
+    # fixed theta over the same steps as each candidate: one evaluation cycle of its interval
+    base = {(v, k): evaluate(val, None, cycle=max(8, k))["plain"] for v, val in enumerate(vals) for k in EVERY}
+    print("validation plain:", {str(k): b for k, b in base.items()}, flush=True)
     best = None
+
+    def consider(model, floor, every, info):
+        nonlocal best
+        model = dict(model)
+        model["theta_min"] = floor
+        model["every"] = every
+        rs = []
+        for v, val in enumerate(vals):
+            r = evaluate(val, model)["learned"]
+            b = base[(v, every)]
+            r.update({"speedup": b["ms_per_step"] / r["ms_per_step"], "p99_ratio": r["p99"] / b["p99"],
+                      "p99_max_ratio": r["p99_max"] / b["p99_max"],
+                      "interaction_gain": b["interactions"] / r["interactions"]})
+            rs.append(r)
+        r = dict(info, theta_min=floor, every=every, loss=float(model.get("loss", 0.0)),
+                 speedup=float(np.mean([x["speedup"] for x in rs])),
+                 interaction_gain=float(np.mean([x["interaction_gain"] for x in rs])),
+                 p99_ratio=float(np.mean([x["p99_ratio"] for x in rs])),
+                 p99_ratio_worst=max(x["p99_ratio"] for x in rs),
+                 p99_max_ratio=float(np.mean([x["p99_max_ratio"] for x in rs])),
+                 ms_per_step=float(np.mean([x["ms_per_step"] for x in rs])), per_seed=rs)
+        print(json.dumps({k: v for k, v in r.items() if k != "per_seed"}), flush=True)
+        if (r["p99_ratio"] <= P99_MARGIN and r["p99_max_ratio"] <= 1.0 and r["p99_ratio_worst"] <= P99_WORST
+                and (best is None or r["speedup"] > best[1]["speedup"])):
+            best = (model, r)
+
+    # the model in place (if any) competes with its inference-time settings re-searched
+    if os.path.exists(args.previous):
+        prev = LR.load_model(args.previous)
+        prev.pop("validation", None)
+        for floor, every in [(f, e) for f in FLOORS for e in EVERY]:
+            consider(prev, floor, every, {"source": "previous model"})
     X = np.concatenate([F.reshape(-1, 12) for F in Fs])
-    for tau_frac in (0.4, 0.5, 0.6, 0.7, 0.8):
+    for tau_frac in TAU_FRACS:
         Y = np.concatenate([np.tile(LR.theta_target(E, tau_frac * p99_plain), E.shape[0]) for E in Es])
-        for q in (0.1, 0.2, 0.3):
-            model = LR.train(X, Y, quantile=q, iters=args.iters)
+        for q, init in [(q, i) for q in QUANTILES for i in INIT_SEEDS]:
+            model = LR.train(X, Y, quantile=q, iters=args.iters, seed=init)
             model.update({"theta_max": 1.0, "tau_frac": tau_frac, "tau": tau_frac * p99_plain,
-                          "group": args.group})
+                          "group": args.group, "init_seed": init})
             # the angle's floor is an inference-time clamp: a floor too low lets a few groups
             # walk at a very small angle, and their long walks become the launch's tail
             for floor, every in [(f, e) for f in FLOORS for e in EVERY]:
-                model["theta_min"] = floor
-                model["every"] = every
-                r = evaluate(val, model)["learned"]
-                r.update({"tau_frac": tau_frac, "quantile": q, "theta_min": floor, "every": every, "loss": model["loss"],
-                          "interaction_gain": base["interactions"] / r["interactions"],
-                          "speedup": base["ms_per_step"] / r["ms_per_step"], "p99_ratio": r["p99"] / base["p99"],
-                          "p99_max_ratio": r["p99_max"] / base["p99_max"]})
-                print(json.dumps(r), flush=True)
-                if (r["p99"] <= base["p99"] and r["p99_max"] <= base["p99_max"]
-                        and (best is None or r["ms_per_step"] < best[1]["ms_per_step"])):
-                    best = (dict(model), r)
+                consider(model, floor, every, {"source": "trained", "tau_frac": tau_frac, "quantile": q,
+                                               "init_seed": init})
     if best is None:
         raise SystemExit("no candidate met the fixed-theta p99 error")
     model, r = best
-    model["validation"] = json.dumps({"plain": base, "learned": r})
+    model["validation"] = json.dumps({"plain": {str(k): b for k, b in base.items()}, "learned": r})
     os.makedirs(os.path.dirname(args.out), exist_ok=True)
     LR.save(model, args.out)
     print("saved %s: %.3fx speed, %.3fx fewer interactions at p99 ratio %.3f (%.0f s)"

@@ -128,8 +128,10 @@ MODEL = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 @pytest.mark.skipif(not os.path.exists(MODEL), reason="trained model not present")
 def test_trained_model_gains_over_fixed_theta():
-    """The committed model on a Plummer sphere it was not trained on: fewer interactions
-    than theta = 0.5 at an equal or lower p99 force error against FP64 (4096 bodies)."""
+    """The committed model on a Plummer sphere it was neither trained nor selected on: fewer
+    interactions than theta = 0.5 at an equal or lower p99 force error against FP64, averaged
+    over one whole evaluation cycle of the model (8 steps, the same steps and the same 16,384
+    sampled bodies for both), and a worst step no worse than fixed theta's worst."""
     import sys
     from nbh import learned as LR
     from nbh import train_theta as TT
@@ -140,4 +142,5 @@ def test_trained_model_gains_over_fixed_theta():
     gain = r["plain"]["interactions"] / r["learned"]["interactions"]
     print("learned-theta gain %.3fx, p99 %.3e vs %.3e" % (gain, r["learned"]["p99"], r["plain"]["p99"]), file=sys.stderr)
     assert gain > 1.05
-    assert r["learned"]["p99"] <= 1.05 * r["plain"]["p99"]
+    assert r["learned"]["p99"] <= r["plain"]["p99"]
+    assert r["learned"]["p99_max"] <= r["plain"]["p99_max"]
