@@ -390,6 +390,8 @@ def main():
                     help="bodies sampled for the FP64 error (the same bodies in both arms, every step)")
     ap.add_argument("--profile-only", action="store_true",
                     help="load, warm up and run the timed steps only (for ncu captures)")
+    ap.add_argument("--profile-learned", action="store_true",
+                    help="a --profile-only run steps with the learned per-body angle")
     ap.add_argument("--force-threads", type=int, default=0,
                     help="force launch geometry of a --profile-only run (0: the library default)")
     ap.add_argument("--stack-cap", type=int, default=0,
@@ -453,6 +455,10 @@ def main():
     # ---- plain fixed theta: warm-up, error of one step, timed steps ---------------------
     sim = new_sim(**({"force_threads": args.force_threads, "stack_cap": args.stack_cap} if args.profile_only else {}))
     args.vote_width = int(sim.config.vote_width)
+    model_path = LR.default_model_path()
+    model = LR.load_model(model_path) if (not args.no_learned and os.path.exists(model_path)) else None
+    if args.profile_only and args.profile_learned and model is not None:
+        LR.install(sim, model)
     stream = torch.cuda.ExternalStream(sim.stream, device=dev)
     for _ in range(args.warmup):
         flush_l2(stream)
@@ -464,8 +470,6 @@ def main():
         args.vote_width = int(tune["vote_width"])
     # the error of both arms over the same steps: one full evaluation cycle of the learned
     # model (every phase of it once), from the same step index
-    model_path = LR.default_model_path()
-    model = LR.load_model(model_path) if (not args.no_learned and os.path.exists(model_path)) else None
     cycle = max(8, int(model.get("every", 1))) if model is not None else 8
     force_error = None if args.profile_only else _cycle_error(sim, idx, cycle, O, np)
     clocks = ClockSampler(local) if rank == 0 else None
@@ -488,7 +492,8 @@ def main():
     # per-stage device times (eager launches with events between stages)
     hbm_peak, peak_src = _peaks()
     geometry = {} if tune is None else {"force_threads": tune["force_threads"], "stack_cap": tune["stack_cap"],
-                                        "build_phases": tune["build_phases"], "build_buckets": tune["build_buckets"]}
+                                        "build_phases": tune["build_phases"], "build_buckets": tune["build_buckets"],
+                                        "top_phase": tune["top_phase"]}
     if tune is not None and args.tune_vote:
         args.vote = int(tune["vote_width"])      # the other sims walk with the chosen width too
     ts = new_sim(stage_timing=True, **geometry)
@@ -647,7 +652,8 @@ def main():
             "stages": stages,
             "roofline": roofline,
             "autotune": None if tune is None else {k: tune[k] for k in (
-                "force_threads", "stack_cap", "build_phases", "build_buckets", "vote_width", "max_depth", "ms_force",
+                "force_threads", "stack_cap", "build_phases", "build_buckets", "top_phase", "vote_width", "max_depth",
+                "ms_force",
                 "ms_force_before",
                 "ms_tree", "ms_tree_before")},
             "e2e": {"value": e2e_ms / div, "unit": "ms/step", "h2d_bytes_per_step": 36 * n,

@@ -180,134 +180,352 @@ constexpr BuildPhase kOnePass[1] = {{1, 0}};
 constexpr BuildPhase kThreePhases[3] = {{256, 0}, {16, 16}, {1, 16}};
 constexpr BuildPhase kFivePhases[5] = {{256, 0}, {64, 4}, {16, 4}, {4, 4}, {1, 4}};
 
+// One body's lock insertion into its universe's tree (see build_kernel).  Returns false
+// after raising an error (depth, pool, timeout).
+__device__ bool lock_insert(const StepParams& p, int b, int u, bool zero_counts, int& local_max, int& waits,
+                            int& misses) {
+    const int nbody = p.nbody;
+    const int root = p.nnodes - u;
+    const float4 rc = p.node4[root];
+    const float radius = p.uradius[u];
+    const float4 bp = p.node4[b];
+    int node = root, depth = 1;
+    float r = radius;
+    float cx = rc.x, cy = rc.y, cz = rc.z;
+    int path = octant(cx, cy, cz, bp.x, bp.y, bp.z);
+    int* slot = cell_child(p, node) + path;
+    // Slots are read through L1 and without acquire, so a read may return an older
+    // value of the slot.  That is safe because of what a slot can have held: the
+    // bbox stage empties every pool slot a build wrote (kNull), and during the
+    // build a slot only goes kNull -> body -> cell, with kLock in between; a cell
+    // index, once stored, stays.  A cell index read is therefore always the
+    // current one, and any other value is only acted on through the CAS below,
+    // which fails if it is stale and returns the current value.  The reset keeps
+    // this true whatever the L1 holds: a sector of a newly taken cell cached before
+    // the cell was initialised can only show kNull, never a child index left by
+    // the previous step's tree.  Reading through L1 keeps the descents off the L2
+    // lines of the top cells.
+    int ch = __ldca(slot);
+    for (;;) {
+        while (ch >= nbody) {                      // :77-89
+            if (ch >= node || depth >= kMaxDepth) {  // children sit below parents
+                raise_error(p.st, NBH_ERR_DEPTH);
+                return false;
+            }
+            node = ch;
+            ++depth;
+            // The child's centre is the one its creator computed (:124-136) from this
+            // centre and half-width, so it is derived here instead of loaded.
+            const float h = r * 0.5f;
+            cx = __fadd_rn(__fsub_rn(cx, h), (path & 1) ? r : 0.0f);
+            cy = __fadd_rn(__fsub_rn(cy, h), (path & 2) ? r : 0.0f);
+            cz = __fadd_rn(__fsub_rn(cz, h), (path & 4) ? r : 0.0f);
+            r = h;
+            path = octant(cx, cy, cz, bp.x, bp.y, bp.z);
+            slot = cell_child(p, node) + path;
+            ch = __ldca(slot);
+        }
+        int seen = kLock;
+        if (ch != kLock && (seen = atomicCAS(slot, ch, kLock)) == ch) {
+            if (ch == kNull) {
+                // nothing but the index itself is published: no fence needed
+                st_relaxed(slot, b);
+            } else {
+                const int old = ch;
+                const float4 op = p.node4[old];
+                int patch = -1, cur = node, cpath = path;
+                for (;;) {
+                    ++depth;
+                    if (depth > kMaxDepth) {
+                        raise_error(p.st, NBH_ERR_DEPTH);
+                        return false;
+                    }
+                    // Cells of the lanes splitting together come from one atomic on
+                    // the shared counter (contiguous, still below every parent).
+                    const unsigned act = __activemask();
+                    const int lane = threadIdx.x & 31;
+                    const int leader = __ffs(act) - 1;
+                    int base = 0;
+                    if (lane == leader) base = atomicSub(&p.st->bottom, __popc(act));
+                    base = __shfl_sync(act, base, leader);
+                    const int cell = base - 1 - __popc(act & ((1u << lane) - 1u));
+                    if (cell <= nbody) {
+                        raise_error(p.st, NBH_ERR_POOL);
+                        return false;
+                    }
+                    const float ox = (cpath & 1) ? r : 0.0f;
+                    const float oy = (cpath & 2) ? r : 0.0f;
+                    const float oz = (cpath & 4) ? r : 0.0f;
+                    r *= 0.5f;
+                    cx = __fadd_rn(__fsub_rn(cx, r), ox);
+                    cy = __fadd_rn(__fsub_rn(cy, r), oy);
+                    cz = __fadd_rn(__fsub_rn(cz, r), oz);
+                    int* cc = cell_child(p, cell);
+                    reinterpret_cast<int4*>(cc)[0] = make_int4(kNull, kNull, kNull, kNull);
+                    reinterpret_cast<int4*>(cc)[1] = make_int4(kNull, kNull, kNull, kNull);
+                    p.arrive[cell - nbody] = 0;
+                    p.clevel[cell - nbody] = depth - 1;   // root = level 0
+                    if (zero_counts) {   // bucket counters of the sampled tree
+                        int4* bc = reinterpret_cast<int4*>(p.kids4 + ((size_t)(cell - nbody) << 3));
+                        bc[0] = make_int4(0, 0, 0, 0);
+                        bc[1] = make_int4(0, 0, 0, 0);
+                    }
+                    if (patch < 0) patch = cell;
+                    else cell_child(p, cur)[cpath] = cell;
+                    const int opath = octant(cx, cy, cz, op.x, op.y, op.z);
+                    cc[opath] = old;
+                    cur = cell;
+                    cpath = octant(cx, cy, cz, bp.x, bp.y, bp.z);
+                    if (cpath != opath) break;
+                }
+                cell_child(p, cur)[cpath] = b;
+                // the new cells' centres and slots become visible before their index
+                st_release(slot, patch);
+            }
+            local_max = max(local_max, depth);
+            break;
+        }
+        if (seen != kLock) {        // the slot moved on: continue from its value
+            if (ch != kLock) ++misses;
+            ch = seen;
+            continue;
+        }
+        // the slot is locked by a split in progress: wait (bounded, backed off)
+        // until it holds the new subtree
+        ch = bounded_wait_ne(slot, kLock, kWaitNs, p.st, kBackoffMinNs, &waits);
+        if (ch == kLock) return false;
+    }
+    return true;
+}
+
 __global__ void __launch_bounds__(256) build_kernel(StepParams p, BuildPhase phase, bool zero_counts) {
     if (load_status(p.st)) return;
     int local_max = 1;
     int waits = 0, misses = 0;
-    const int nbody = p.nbody;
     const int per = phase_bodies(phase);
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;   // one body per thread
     if (g < (long long)p.nchunks * per) {
         const int4 ck = p.chunks[g / per];
         const int b = ck.y + phase_offset(phase, (int)(g % per), g / per);
-        if (b < ck.z) {
-            const int root = p.nnodes - ck.x;
-            const float4 rc = p.node4[root];
-            const float radius = p.uradius[ck.x];
+        if (b < ck.z) lock_insert(p, b, ck.x, zero_counts, local_max, waits, misses);
+    }
+    // :199; the maximum persists across steps, so the atomic is rarely needed
+    if (local_max > ld_relaxed(&p.st->max_depth)) atomicMax(&p.st->max_depth, local_max);
+    if (waits) atomicAdd(&p.st->lock_waits[blockIdx.x % kDiagSlots], waits);
+    if (misses) atomicAdd(&p.st->cas_misses[blockIdx.x % kDiagSlots], misses);
+}
+
+// -------------------------------------------------------------------------------------
+// The first insertion phase (one body of every 256-body chunk) in shared memory.  On an
+// empty tree that phase is the slowest one: every sampled body of a universe descends into
+// the same few top slots at once and waits on each split there in turn, through global
+// locks and release fences.  Here one block per universe builds those top levels in its
+// shared memory instead -- the same descents, the same centre arithmetic and the same CAS
+// locks, but on shared slots, where a lock round trip takes tens of cycles -- and then
+// publishes them: the new cells are taken from the pool with one atomic and every slot is
+// written once with its final value.  The tree is the one the global phase builds (an
+// octree does not depend on insertion order).  Cells are numbered in the order they are
+// made, and every cell is made after its parent, so the pool indices stay below their
+// parents'.  If the sample needs more cells than the block holds, or a split goes deeper
+// than the depth limit, the block inserts its sample through the global locks instead.
+//
+// Shared slots hold 16-bit values: a local cell (kTopCell | index), a sample (its index
+// within the universe's chunks), kTopNull or kTopLock.  Every slot is emptied before the
+// first descent, so a slot read before the write that fills it can only show kTopNull, and
+// acting on that goes through the CAS, which fails and returns the current value.
+constexpr int kTopThreads = 1024;
+constexpr int kTopCells = 12288;
+constexpr unsigned short kTopNull = 0xffffu, kTopLock = 0xfffeu, kTopCell = 0x8000u;
+constexpr BuildPhase kFirstPhase = {256, 0};
+constexpr long long kTopSpin = 1ll << 22;     // polls of a locked shared slot before giving up
+
+constexpr int kTopMaxSamples = 0x7ffe;       // sample indices stay below kTopLock and kTopCell
+int top_build_max_samples() { return kTopMaxSamples; }
+size_t top_build_smem() { return (size_t)kTopCells * 8 * sizeof(unsigned short) + kTopCells; }
+
+__device__ __forceinline__ unsigned short ld_shared_volatile(const unsigned short* a) {
+    return *reinterpret_cast<const volatile unsigned short*>(a);
+}
+
+__global__ void __launch_bounds__(kTopThreads) top_build_kernel(StepParams p, bool zero_counts) {
+    extern __shared__ __align__(16) unsigned char top_smem[];
+    unsigned short* slots = reinterpret_cast<unsigned short*>(top_smem);          // [kTopCells][8]
+    unsigned char* lvl = top_smem + (size_t)kTopCells * 8 * sizeof(unsigned short);
+    __shared__ int ncell, failed, c0, gbase, depth_max, status;
+    // one read of the status word for the whole block: threads that saw different values
+    // would part at the barriers below
+    if (threadIdx.x == 0) status = load_status(p.st);
+    __syncthreads();
+    if (status) return;
+    const int u = blockIdx.x;
+    const int nbody = p.nbody;
+    const int nsamp = (p.ubody[u + 1] - p.ubody[u] + 255) / 256;    // chunks of universe u
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = p.nchunks;              // first chunk of universe u
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (p.chunks[mid].x < u) lo = mid + 1;
+            else hi = mid;
+        }
+        c0 = lo;
+        ncell = 1;                               // local cell 0 is the root
+        failed = nsamp > kTopMaxSamples ? 1 : 0;
+        depth_max = 1;
+        lvl[0] = 0;
+    }
+    for (int i = threadIdx.x; i < kTopCells * 4; i += blockDim.x) reinterpret_cast<unsigned*>(slots)[i] = 0xffffffffu;
+    __syncthreads();
+    const int root = p.nnodes - u;
+    const float4 rc = p.node4[root];
+    const float radius = p.uradius[u];
+    int local_max = 1;
+    if (!failed) {
+        for (int smp = threadIdx.x; smp < nsamp; smp += blockDim.x) {
+            const long long ci = c0 + smp;
+            const int4 ck = p.chunks[ci];
+            const int b = ck.y + phase_offset(kFirstPhase, 0, ci);
+            if (b >= ck.z) continue;
             const float4 bp = p.node4[b];
-            int node = root, depth = 1;
-            float r = radius;
-            float cx = rc.x, cy = rc.y, cz = rc.z;
+            int node = 0, depth = 1;
+            float r = radius, cx = rc.x, cy = rc.y, cz = rc.z;
             int path = octant(cx, cy, cz, bp.x, bp.y, bp.z);
-            int* slot = cell_child(p, node) + path;
-            // Slots are read through L1 and without acquire, so a read may return an older
-            // value of the slot.  That is safe because of what a slot can have held: the
-            // bbox stage empties every pool slot a build wrote (kNull), and during the
-            // build a slot only goes kNull -> body -> cell, with kLock in between; a cell
-            // index, once stored, stays.  A cell index read is therefore always the
-            // current one, and any other value is only acted on through the CAS below,
-            // which fails if it is stale and returns the current value.  The reset keeps
-            // this true whatever the L1 holds: a sector of a newly taken cell cached before
-            // the cell was initialised can only show kNull, never a child index left by
-            // the previous step's tree.  Reading through L1 keeps the descents off the L2
-            // lines of the top cells.
-            int ch = __ldca(slot);
-            for (;;) {
-                while (ch >= nbody) {                      // :77-89
-                    if (ch >= node || depth >= kMaxDepth) {  // children sit below parents
-                        raise_error(p.st, NBH_ERR_DEPTH);
-                        goto finish;
+            unsigned short* slot = slots + node * 8 + path;
+            unsigned short ch = ld_shared_volatile(slot);
+            bool done = false;
+            long long spins = 0;
+            while (!done) {
+                while (ch != kTopNull && ch != kTopLock && (ch & kTopCell)) {
+                    if (depth >= kMaxDepth) {
+                        atomicExch(&failed, 1);
+                        break;
                     }
-                    node = ch;
+                    node = ch & 0x7fff;
                     ++depth;
-                    // The child's centre is the one its creator computed (:124-136) from this
-                    // centre and half-width, so it is derived here instead of loaded.
                     const float h = r * 0.5f;
                     cx = __fadd_rn(__fsub_rn(cx, h), (path & 1) ? r : 0.0f);
                     cy = __fadd_rn(__fsub_rn(cy, h), (path & 2) ? r : 0.0f);
                     cz = __fadd_rn(__fsub_rn(cz, h), (path & 4) ? r : 0.0f);
                     r = h;
                     path = octant(cx, cy, cz, bp.x, bp.y, bp.z);
-                    slot = cell_child(p, node) + path;
-                    ch = __ldca(slot);
+                    slot = slots + node * 8 + path;
+                    ch = ld_shared_volatile(slot);
                 }
-                int seen = kLock;
-                if (ch != kLock && (seen = atomicCAS(slot, ch, kLock)) == ch) {
-                    if (ch == kNull) {
-                        // nothing but the index itself is published: no fence needed
-                        st_relaxed(slot, b);
-                    } else {
-                        const int old = ch;
-                        const float4 op = p.node4[old];
-                        int patch = -1, cur = node, cpath = path;
-                        for (;;) {
-                            ++depth;
-                            if (depth > kMaxDepth) {
-                                raise_error(p.st, NBH_ERR_DEPTH);
-                                goto finish;
-                            }
-                            // Cells of the lanes splitting together come from one atomic on
-                            // the shared counter (contiguous, still below every parent).
-                            const unsigned act = __activemask();
-                            const int lane = threadIdx.x & 31;
-                            const int leader = __ffs(act) - 1;
-                            int base = 0;
-                            if (lane == leader) base = atomicSub(&p.st->bottom, __popc(act));
-                            base = __shfl_sync(act, base, leader);
-                            const int cell = base - 1 - __popc(act & ((1u << lane) - 1u));
-                            if (cell <= nbody) {
-                                raise_error(p.st, NBH_ERR_POOL);
-                                goto finish;
-                            }
-                            const float ox = (cpath & 1) ? r : 0.0f;
-                            const float oy = (cpath & 2) ? r : 0.0f;
-                            const float oz = (cpath & 4) ? r : 0.0f;
-                            r *= 0.5f;
-                            cx = __fadd_rn(__fsub_rn(cx, r), ox);
-                            cy = __fadd_rn(__fsub_rn(cy, r), oy);
-                            cz = __fadd_rn(__fsub_rn(cz, r), oz);
-                            int* cc = cell_child(p, cell);
-                            reinterpret_cast<int4*>(cc)[0] = make_int4(kNull, kNull, kNull, kNull);
-                            reinterpret_cast<int4*>(cc)[1] = make_int4(kNull, kNull, kNull, kNull);
-                            p.arrive[cell - nbody] = 0;
-                            p.clevel[cell - nbody] = depth - 1;   // root = level 0
-                            if (zero_counts) {   // bucket counters of the sampled tree
-                                int4* bc = reinterpret_cast<int4*>(p.kids4 + ((size_t)(cell - nbody) << 3));
-                                bc[0] = make_int4(0, 0, 0, 0);
-                                bc[1] = make_int4(0, 0, 0, 0);
-                            }
-                            if (patch < 0) patch = cell;
-                            else cell_child(p, cur)[cpath] = cell;
-                            const int opath = octant(cx, cy, cz, op.x, op.y, op.z);
-                            cc[opath] = old;
-                            cur = cell;
-                            cpath = octant(cx, cy, cz, bp.x, bp.y, bp.z);
-                            if (cpath != opath) break;
-                        }
-                        cell_child(p, cur)[cpath] = b;
-                        // the new cells' centres and slots become visible before their index
-                        st_release(slot, patch);
+                if (*reinterpret_cast<volatile int*>(&failed)) break;
+                if (ch == kTopLock) {                  // a split in progress: wait, bounded
+                    if (++spins > kTopSpin) {
+                        raise_error(p.st, NBH_ERR_TIMEOUT);
+                        atomicExch(&failed, 2);
+                        break;
                     }
-                    local_max = max(local_max, depth);
-                    break;
+                    __nanosleep(32);
+                    ch = ld_shared_volatile(slot);
+                    continue;
                 }
-                if (seen != kLock) {        // the slot moved on: continue from its value
-                    if (ch != kLock) ++misses;
+                const unsigned short seen = atomicCAS(slot, ch, kTopLock);
+                if (seen != ch) {
                     ch = seen;
                     continue;
                 }
-                // the slot is locked by a split in progress: wait (bounded, backed off)
-                // until it holds the new subtree
-                ch = bounded_wait_ne(slot, kLock, kWaitNs, p.st, kBackoffMinNs, &waits);
-                if (ch == kLock) goto finish;
+                if (ch == kTopNull) {
+                    *reinterpret_cast<volatile unsigned short*>(slot) = (unsigned short)smp;
+                    local_max = max(local_max, depth);
+                    done = true;
+                    break;
+                }
+                // split: the slot held sample `ch`; cells until the two separate
+                const int4 ock = p.chunks[c0 + ch];
+                const float4 op = p.node4[ock.y + phase_offset(kFirstPhase, 0, c0 + ch)];
+                int patch = -1, cur = node, cpath = path;
+                bool ok = true;
+                for (;;) {
+                    ++depth;
+                    const int cell = atomicAdd(&ncell, 1);
+                    if (depth > kMaxDepth || cell >= kTopCells) {
+                        atomicExch(&failed, 1);
+                        ok = false;
+                        break;
+                    }
+                    const float ox = (cpath & 1) ? r : 0.0f;
+                    const float oy = (cpath & 2) ? r : 0.0f;
+                    const float oz = (cpath & 4) ? r : 0.0f;
+                    r *= 0.5f;
+                    cx = __fadd_rn(__fsub_rn(cx, r), ox);
+                    cy = __fadd_rn(__fsub_rn(cy, r), oy);
+                    cz = __fadd_rn(__fsub_rn(cz, r), oz);
+                    lvl[cell] = (unsigned char)(depth - 1);
+                    if (patch < 0) patch = cell;
+                    else slots[cur * 8 + cpath] = (unsigned short)(kTopCell | cell);
+                    const int opath = octant(cx, cy, cz, op.x, op.y, op.z);
+                    slots[cell * 8 + opath] = ch;
+                    cur = cell;
+                    cpath = octant(cx, cy, cz, bp.x, bp.y, bp.z);
+                    if (cpath != opath) break;
+                }
+                if (!ok) break;
+                slots[cur * 8 + cpath] = (unsigned short)smp;
+                __threadfence_block();                 // the new cells before their index
+                *reinterpret_cast<volatile unsigned short*>(slot) = (unsigned short)(kTopCell | patch);
+                local_max = max(local_max, depth);
+                done = true;
             }
         }
     }
-finish:
-    // :199; the maximum persists across steps, so the atomic is rarely needed
-    if (local_max > ld_relaxed(&p.st->max_depth)) atomicMax(&p.st->max_depth, local_max);
-    if (waits) atomicAdd(&p.st->lock_waits[blockIdx.x % kDiagSlots], waits);
-    if (misses) atomicAdd(&p.st->cas_misses[blockIdx.x % kDiagSlots], misses);
+    atomicMax(&depth_max, local_max);
+    __syncthreads();
+    if (failed == 2) return;                           // a wait gave up: the status says so
+    if (failed) {
+        // more cells than the block holds, or a very deep split: the global lock insertion
+        int lm = 1, waits = 0, misses = 0;
+        for (int smp = threadIdx.x; smp < nsamp; smp += blockDim.x) {
+            const long long ci = c0 + smp;
+            const int4 ck = p.chunks[ci];
+            const int b = ck.y + phase_offset(kFirstPhase, 0, ci);
+            if (b < ck.z && !lock_insert(p, b, u, zero_counts, lm, waits, misses)) break;
+        }
+        if (lm > ld_relaxed(&p.st->max_depth)) atomicMax(&p.st->max_depth, lm);
+        if (waits) atomicAdd(&p.st->lock_waits[blockIdx.x % kDiagSlots], waits);
+        if (misses) atomicAdd(&p.st->cas_misses[blockIdx.x % kDiagSlots], misses);
+        return;
+    }
+    // publish: local cell c (c >= 1) becomes pool cell gbase - c
+    const int nc = ncell;
+    if (threadIdx.x == 0) {
+        gbase = nc > 1 ? atomicSub(&p.st->bottom, nc - 1) : 0;
+        status = 0;
+        if (nc > 1 && gbase - (nc - 1) <= nbody) {
+            raise_error(p.st, NBH_ERR_POOL);
+            status = NBH_ERR_POOL;
+        }
+        if (depth_max > ld_relaxed(&p.st->max_depth)) atomicMax(&p.st->max_depth, depth_max);
+    }
+    __syncthreads();
+    if (status) return;
+    const int gb = gbase;
+    for (int i = threadIdx.x; i < nc * 8; i += blockDim.x) {
+        const int c = i >> 3;
+        const unsigned short v = slots[i];
+        int g = kNull;
+        if (v != kTopNull) {
+            if (v & kTopCell) {
+                g = gb - (v & 0x7fff);
+            } else {
+                const long long ci = c0 + v;
+                g = p.chunks[ci].y + phase_offset(kFirstPhase, 0, ci);
+            }
+        }
+        const int gc = c == 0 ? root : gb - c;
+        cell_child(p, gc)[i & 7] = g;
+    }
+    for (int c = 1 + (int)threadIdx.x; c < nc; c += blockDim.x) {
+        const int k = gb - c - nbody;
+        p.arrive[k] = 0;
+        p.clevel[k] = lvl[c];
+        if (zero_counts) {   // bucket counters of the sampled tree
+            int4* bc = reinterpret_cast<int4*>(p.kids4 + ((size_t)k << 3));
+            bc[0] = make_int4(0, 0, 0, 0);
+            bc[1] = make_int4(0, 0, 0, 0);
+        }
+    }
 }
 
 // -------------------------------------------------------------------------------------
@@ -1018,13 +1236,22 @@ static void launch_bucket_pass(const StepParams& p, BuildPhase set, bool first, 
     bucket_build_kernel<<<kBucketBlocksPerSm * sms, 32 * kBucketWarps, 0, s>>>(p, zero_counts);
 }
 
-void launch_build(const StepParams& p, int phases, bool buckets, int sms, cudaStream_t s) {
+// The first phase (one body per chunk) of the multi-phase schedules: in shared memory (one
+// block per universe) when `top`, else through the global locks.
+static void launch_first_phase(const StepParams& p, bool zero_counts, bool top, cudaStream_t s) {
+    if (top)
+        top_build_kernel<<<p.nuniv, kTopThreads, top_build_smem(), s>>>(p, zero_counts);
+    else
+        build_kernel<<<(unsigned)((p.nchunks * (long long)phase_bodies(kFirstPhase) + 255) / 256), 256, 0, s>>>(
+            p, kFirstPhase, zero_counts);
+}
+
+void launch_build(const StepParams& p, int phases, bool buckets, int sms, bool top, cudaStream_t s) {
     buckets = buckets && phases != 1;
     if (buckets && phases == 3) {
         // one lock phase (1/256 of each chunk), then the rest of the 1/16 sample as bucket
         // subtrees of that tree, then every other body as bucket subtrees of the sample's
-        build_kernel<<<(unsigned)((p.nchunks * (long long)phase_bodies(kThreePhases[0]) + 255) / 256), 256, 0, s>>>(
-            p, kThreePhases[0], true);
+        launch_first_phase(p, true, top, s);
         launch_bucket_pass(p, kThreePhases[1], true, true, sms, s);
         launch_bucket_pass(p, kBucketBodies, false, false, sms, s);
         return;
@@ -1033,10 +1260,18 @@ void launch_build(const StepParams& p, int phases, bool buckets, int sms, cudaSt
     int count = phases == 1 ? 1 : (phases == 5 ? 5 : 3);
     if (buckets) count -= 2;   // five phases: the lock phases insert the 1/16 sample only
     for (int k = 0; k < count; ++k) {
+        if (k == 0 && phases != 1) {
+            launch_first_phase(p, buckets, top, s);
+            continue;
+        }
         const long long bodies = (long long)p.nchunks * phase_bodies(sched[k]);
         build_kernel<<<(unsigned)((bodies + 255) / 256), 256, 0, s>>>(p, sched[k], buckets);
     }
     if (buckets) launch_bucket_pass(p, kBucketBodies, true, false, sms, s);
+}
+
+cudaError_t prepare_tree_kernels() {
+    return cudaFuncSetAttribute(top_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)top_build_smem());
 }
 
 size_t bucket_stack_bytes(int sms) {

@@ -45,7 +45,7 @@ class NbhConfig(C.Structure):
         ("vote_width", C.c_int32), ("arith", C.c_int32), ("precise", C.c_int32),
         ("stage_timing", C.c_int32), ("use_graph", C.c_int32), ("force_threads", C.c_int32),
         ("stack_cap", C.c_int32), ("build_phases", C.c_int32), ("build_buckets", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("top_phase", C.c_int32), ("reserved", C.c_int32 * 3),
     ]
 
 
@@ -82,7 +82,7 @@ class NbhTune(C.Structure):
         ("ms_tree", C.c_float), ("ms_tree_before", C.c_float), ("trials", C.c_int32),
         ("trial_kind", C.c_int32 * NBH_TUNE_MAX_TRIALS), ("trial_a", C.c_int32 * NBH_TUNE_MAX_TRIALS),
         ("trial_b", C.c_int32 * NBH_TUNE_MAX_TRIALS), ("trial_vote", C.c_int32 * NBH_TUNE_MAX_TRIALS),
-        ("trial_ms", C.c_float * NBH_TUNE_MAX_TRIALS),
+        ("trial_ms", C.c_float * NBH_TUNE_MAX_TRIALS), ("top_phase", C.c_int32),
     ]
 
 

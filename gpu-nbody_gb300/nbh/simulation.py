@@ -35,7 +35,7 @@ def _f32(a):
 def make_config(theta=0.5, eps=0.05, dt=0.025, G=1.0, pool_factor=2.0, vote_width=None,
                 arith=L.NBH_ARITH_FMA, precise=False, stage_timing=False, use_graph=True,
                 device=0, theta2=0.0, eps2=0.0, force_threads=0, stack_cap=0, build_phases=0,
-                build_buckets=0) -> L.NbhConfig:
+                build_buckets=0, top_phase=0) -> L.NbhConfig:
     cfg = L.NbhConfig()
     L.load().nbh_config_default(C.byref(cfg))
     cfg.device = device
@@ -50,6 +50,7 @@ def make_config(theta=0.5, eps=0.05, dt=0.025, G=1.0, pool_factor=2.0, vote_widt
     cfg.use_graph = int(bool(use_graph))
     cfg.force_threads, cfg.stack_cap, cfg.build_phases = force_threads, stack_cap, build_phases
     cfg.build_buckets = build_buckets
+    cfg.top_phase = top_phase
     return cfg
 
 
@@ -213,7 +214,7 @@ class Simulation:
         trials = [{"kind": ("force", "tree")[t.trial_kind[k]], "a": t.trial_a[k], "b": t.trial_b[k],
                    "vote": t.trial_vote[k], "ms": t.trial_ms[k]} for k in range(t.trials)]
         return {"force_threads": t.force_threads, "stack_cap": t.stack_cap, "build_phases": t.build_phases,
-                "build_buckets": t.build_buckets, "vote_width": t.vote_width,
+                "build_buckets": t.build_buckets, "top_phase": t.top_phase, "vote_width": t.vote_width,
                 "max_depth": t.max_depth, "ms_force": t.ms_force, "ms_force_before": t.ms_force_before,
                 "ms_tree": t.ms_tree, "ms_tree_before": t.ms_tree_before, "trials": trials}
 

@@ -96,7 +96,15 @@ typedef struct nbh_config {
                               warp without locks (the same tree); with 3 phases one lock
                               phase inserts 1/256 and two such passes add the rest of the
                               sample, then the other bodies; 2: lock insertion only */
-    int32_t reserved[4];
+    int32_t top_phase;     /* the first phase of a 3- or 5-phase schedule (one body of every
+                              256) builds the top levels of each universe's tree in shared
+                              memory, one block per universe, and publishes them (the same
+                              tree): 0 (default) where every universe has at most 2048 * 256
+                              bodies (many small universes: faster; one large universe: one
+                              block is too little parallelism), 1 wherever every universe has
+                              at most 32766 * 256 bodies, 2 never (global locks);
+                              nbh_autotune times both where possible */
+    int32_t reserved[3];
 } nbh_config;
 
 /* Fills *cfg with the defaults: theta 0.5, eps 0.05, dt 0.025, G 1, pool 2.0,
@@ -281,8 +289,10 @@ typedef struct nbh_tune {
     int32_t trial_kind[NBH_TUNE_MAX_TRIALS];    /* 0 force, 1 tree */
     int32_t trial_a[NBH_TUNE_MAX_TRIALS];       /* threads, or insertion phases */
     int32_t trial_b[NBH_TUNE_MAX_TRIALS];       /* stack capacity (force), or bucketed (tree) */
-    int32_t trial_vote[NBH_TUNE_MAX_TRIALS];    /* vote width (force) */
+    int32_t trial_vote[NBH_TUNE_MAX_TRIALS];    /* vote width (force), or 1 when the first phase
+                                                   built in shared memory (tree) */
     float   trial_ms[NBH_TUNE_MAX_TRIALS];      /* mean of 3 timed launches after 1 warm-up */
+    int32_t top_phase;             /* chosen: 1 first phase in shared memory, 2 global locks */
 } nbh_tune;
 int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out);
 

@@ -38,7 +38,7 @@ def test_config_struct_layout_matches_header():
     assert (cfg.theta, cfg.G, cfg.pool_factor) == (0.5, 1.0, 2.0)
     assert cfg.eps == pytest.approx(0.05) and cfg.dt == pytest.approx(0.025)
     assert cfg.vote_width == 64 and cfg.arith == L.NBH_ARITH_FMA and cfg.use_graph == 1
-    assert C.sizeof(L.NbhConfig) == 4 * (2 + 7 + 9 + 4)
+    assert C.sizeof(L.NbhConfig) == 4 * (2 + 7 + 10 + 3)
 
 
 def test_struct_layouts_match_the_c_compiler(tmp_path):
