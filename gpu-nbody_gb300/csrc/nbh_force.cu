@@ -430,32 +430,38 @@ void launch_force(const StepParams& p, int vote, bool ref, bool feat, int grid, 
     }
 }
 
-// Resident blocks per SM of the fixed-angle variant at this geometry (the per-body
-// variants use as many registers or fewer per resident warp budget; their grid is the same).
 // Order of the force work items for the next step: longest walks first (longest-
 // processing-time first), so the few long walks -- bodies near a dense centre, or small
 // per-body angles -- start early instead of running alone at the end of the launch.  A
-// counting sort by floor(log2(cost)), descending; within a class the order is arbitrary.
-// One block; warp-aggregated shared-memory atomics.
+// counting sort by cost class, descending: four classes per power of two (the two bits
+// below the leading one), so that items of one class differ by at most 19 %; within a
+// class the order is arbitrary.  One block; warp-aggregated shared-memory atomics.
 constexpr int kOrderThreads = 1024;
+constexpr int kOrderClasses = 128;
+__device__ __forceinline__ int cost_class(int c) {
+    c = max(c, 1);
+    const int e = 31 - __clz(c);
+    const int frac = e >= 2 ? (c >> (e - 2)) & 3 : (c << (2 - e)) & 3;
+    return 4 * e + frac;
+}
 __global__ void __launch_bounds__(kOrderThreads) item_order_kernel(const int* __restrict__ cost, int nitems,
                                                                    int* order) {
-    __shared__ int cnt[32], off[32];
+    __shared__ int cnt[kOrderClasses], off[kOrderClasses];
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    if (threadIdx.x < 32) cnt[threadIdx.x] = 0;
+    if (threadIdx.x < kOrderClasses) cnt[threadIdx.x] = 0;
     __syncthreads();
     for (int i0 = 0; i0 < nitems; i0 += blockDim.x) {
         const int i = i0 + threadIdx.x;
         const bool v = i < nitems;
-        const int cls = v ? 31 - __clz(max(cost[i], 1)) : -1;
+        const int cls = v ? cost_class(cost[i]) : -1;
         const unsigned grp = __match_any_sync(0xffffffffu, cls);
         if (v && lane == __ffs(grp) - 1) atomicAdd(&cnt[cls], __popc(grp));
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         int sum = 0;
-        for (int c = 31; c >= 0; --c) {
+        for (int c = kOrderClasses - 1; c >= 0; --c) {
             off[c] = sum;
             sum += cnt[c];
         }
@@ -464,7 +470,7 @@ __global__ void __launch_bounds__(kOrderThreads) item_order_kernel(const int* __
     for (int i0 = 0; i0 < nitems; i0 += blockDim.x) {
         const int i = i0 + threadIdx.x;
         const bool v = i < nitems;
-        const int cls = v ? 31 - __clz(max(cost[i], 1)) : -1;
+        const int cls = v ? cost_class(cost[i]) : -1;
         const unsigned grp = __match_any_sync(0xffffffffu, cls);
         const int leader = __ffs(grp) - 1;
         int base = 0;
