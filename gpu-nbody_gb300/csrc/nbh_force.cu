@@ -97,12 +97,8 @@ __device__ __forceinline__ float dist2(const float dx, const float dy, const flo
 // results go to p.probe (x, y, z, bound) and no body state changes (force probe).  With
 // p.feat_gate set, a launch that does not match the step's place in the learned-theta
 // schedule returns at once (the step graph holds a recording and a plain launch).
-// At least 3 resident blocks of the largest geometry: the compiler then keeps up to 85
-// registers per thread, and the 64-wide walks are compiled to 63-64 registers without
-// spills (left to itself it compiles the per-body-angle walk to 48, with less overlap in
-// the visit loop: 1.6 % slower, the fixed-angle walk 0.7 % slower).
 template <int W, bool REF, bool PB, bool FEAT>
-__global__ void __launch_bounds__(kForceThreadsMax, 3) force_kernel(StepParams p) {
+__device__ __forceinline__ void force_walk(const StepParams& p) {
     if (load_status(p.st)) return;
     if (p.feat_gate && theta_bound_step(p.st, p.st->step) != (p.feat_gate == 1)) return;
     constexpr int GL = group_lanes<W>();            // lanes per group
@@ -365,12 +361,33 @@ __global__ void __launch_bounds__(kForceThreadsMax, 3) force_kernel(StepParams p
     if (lane == 0 && my_inter) atomicAdd(&p.st->interactions, my_inter);
 }
 
+// The kernels.  The 64-wide walks ask for at least 3 resident blocks of the largest
+// geometry: the compiler then keeps up to 85 registers per thread and compiles them to
+// 63-64 registers without spills (left to itself it compiles the per-body-angle walk to 48,
+// with less overlap in the visit loop: 1.6 % slower, the fixed-angle walk 0.7 % slower).
+// The other widths keep the compiler's own choice (with the same hint the 32-wide walk ran
+// 5-10 % slower).
+template <int W, bool REF, bool PB, bool FEAT>
+__global__ void __launch_bounds__(kForceThreadsMax) force_kernel(StepParams p) {
+    force_walk<W, REF, PB, FEAT>(p);
+}
+template <bool PB, bool FEAT>
+__global__ void __launch_bounds__(kForceThreadsMax, 3) force_kernel64(StepParams p) {
+    force_walk<64, false, PB, FEAT>(p);
+}
+
+template <int W, bool REF, bool PB, bool FEAT>
+static auto force_entry() {
+    if constexpr (W == 64 && !REF) return force_kernel64<PB, FEAT>;
+    else return force_kernel<W, REF, PB, FEAT>;
+}
+
 // -------------------------------------------------------------------------------------
 template <int W, bool REF, bool PB>
 static void launch_force_pf(const StepParams& p, bool feat, int grid, int threads, cudaStream_t s) {
     const size_t sm = force_smem_bytes<W>(threads, p.stack_cap);
-    if (feat) force_kernel<W, REF, PB, true><<<grid, threads, sm, s>>>(p);
-    else force_kernel<W, REF, PB, false><<<grid, threads, sm, s>>>(p);
+    if (feat) force_entry<W, REF, PB, true>()<<<grid, threads, sm, s>>>(p);
+    else force_entry<W, REF, PB, false>()<<<grid, threads, sm, s>>>(p);
 }
 
 template <int W, bool REF>
@@ -382,7 +399,7 @@ static void launch_force_t(const StepParams& p, bool pb, bool feat, int grid, in
 // Every variant may be launched with up to the largest geometry's shared memory.
 template <int W, bool REF, bool PB, bool FEAT>
 static cudaError_t prep_force() {
-    return cudaFuncSetAttribute(force_kernel<W, REF, PB, FEAT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(force_entry<W, REF, PB, FEAT>(), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)force_smem_bytes<W>(kForceThreadsMax, kStackCapMax));
 }
 
@@ -459,12 +476,24 @@ __global__ void __launch_bounds__(kOrderThreads) item_order_kernel(const int* __
         if (v && lane == __ffs(grp) - 1) atomicAdd(&cnt[cls], __popc(grp));
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        int sum = 0;
-        for (int c = kOrderClasses - 1; c >= 0; --c) {
-            off[c] = sum;
-            sum += cnt[c];
+    if (threadIdx.x < 32) {
+        // first position of each class, largest costs first: lane l holds classes
+        // 127 - 4l .. 124 - 4l; a warp scan of the lanes' sums
+        static_assert(kOrderClasses == 128, "four classes per lane");
+        const int c0 = kOrderClasses - 1 - 4 * lane;
+        const int n0 = cnt[c0], n1 = cnt[c0 - 1], n2 = cnt[c0 - 2], n3 = cnt[c0 - 3];
+        const int mine = n0 + n1 + n2 + n3;
+        int incl = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
         }
+        const int base = incl - mine;
+        off[c0] = base;
+        off[c0 - 1] = base + n0;
+        off[c0 - 2] = base + n0 + n1;
+        off[c0 - 3] = base + n0 + n1 + n2;
     }
     __syncthreads();
     for (int i0 = 0; i0 < nitems; i0 += blockDim.x) {
@@ -499,7 +528,7 @@ int occupancy_force(int vote, bool ref, int threads, int cap, int* blocks_per_sm
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<128, false, false, false>,
                                                              threads, force_smem_bytes<128>(threads, cap));
     if (vote == 64)
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<64, false, false, false>,
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_entry<64, false, false, false>(),
                                                              threads, force_smem_bytes<64>(threads, cap));
     if (vote == 16)
         return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<16, true, false, false>,
