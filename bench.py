@@ -58,7 +58,7 @@ HBM_FALLBACK_GBS = 6800.0
 # DRAM bytes (read + write) of one force launch (vote width 64) on the 1,048,576-body
 # Plummer workload, from one full ncu capture of that launch (dram__bytes_read.sum +
 # dram__bytes_write.sum).
-FORCE_TRAFFIC_BYTES_1M = 206_981_120 + 24_052_480
+FORCE_TRAFFIC_BYTES_1M = 226_876_672 + 25_779_456
 
 # Algorithmic bytes per body / per cell of the memory-bound stages (minimum traffic:
 # every byte read and written once).
@@ -516,7 +516,8 @@ def main():
     fp32 = __import__("ctypes").c_double()
     nbh._lib.check(nbh._lib.load().nbh_measure_fp32_peak(local, __import__("ctypes").byref(fp32)))
     achieved = FLOPS_PER_INTERACTION * inter_ts / (force_ms * 1e-3) / 1e12
-    roofline = {"bound": "fp32", "kernel": "force_kernel<%d,FMA>" % args.vote_width, "achieved": achieved,
+    kname = "force_kernel64" if args.vote_width == 64 else "force_kernel<%d,FMA>" % args.vote_width
+    roofline = {"bound": "fp32", "kernel": kname, "achieved": achieved,
                 "peak": fp32.value, "unit": "TFLOP/s", "frac": achieved / fp32.value,
                 "traffic": FORCE_TRAFFIC_BYTES_1M if (args.workload == "plummer" and n == 1 << 20
                                                       and args.vote_width == DEFAULT_VOTE) else None,
