@@ -122,6 +122,24 @@ def test_per_body_theta_walk_matches_oracle(vote, group):
     np.testing.assert_allclose(eb, o.ebound(), rtol=1e-4, atol=1e-12)
 
 
+def test_theta_stage_is_timed_on_its_own():
+    """With stage timing, the learned-angle stage (features + MLP) gets its own time: zero
+    without a model, positive with one, and part of the step's time."""
+    n = 20000
+    arrs = plummer(n, seed=6)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, stage_timing=True)
+    g.load(*arrs)
+    g.step(2)
+    st = g.stats()
+    assert st["ms_theta"] < 0.01 and st["ms_sort"] > 0
+    from nbh import learned as LR
+    LR.install(g, _model(5), every=1)
+    g.step(3)
+    st = g.stats()
+    assert 0 < st["ms_theta"] < st["ms_step"]
+    assert st["ms_bbox"] + st["ms_build"] + st["ms_summarize"] + st["ms_sort"] + st["ms_theta"] <= st["ms_step"] * 1.001
+
+
 MODEL = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gpu-nbody_gb300", "nbh",
                      "models", "theta_plummer.npz")
 

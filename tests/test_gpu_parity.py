@@ -526,6 +526,36 @@ def test_long_run_keeps_every_tree_whole():
     g.close()
 
 
+def test_long_run_of_a_batch_with_the_first_phase_in_shared_memory():
+    """200 steps of 64 moving Plummer universes (1K-64K bodies) with the first insertion
+    phase built in shared memory every step: every 50 steps each universe's tree reaches
+    each of its bodies once from its root, the depth-first order is a permutation inside
+    each universe's range, the state is finite and no step reports an error."""
+    import bench
+    from nbh import universe as U
+    counts = bench.ensemble_counts(64, 7)
+    parts = [U.PlummerUniverseGenerator(seed=700 + u).arrays(int(c)) for u, c in enumerate(counts)]
+    cat = [np.concatenate([p[k] for p in parts]) for k in range(7)]
+    n = int(counts.sum())
+    offs = np.concatenate([[0], np.cumsum(counts)])
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, top_phase=1)
+    g.load_batch(counts, *cat)
+    for s in range(4):
+        g.step(50)
+        assert g.stats()["status"] == 0
+        t = g.tree()
+        roots = t["nnodes"] - np.arange(counts.size)
+        reach = _reachable_bodies(t, n, roots)
+        assert reach.size == n and np.unique(reach).size == n, s
+        srt = t["sorted"]
+        for u in range(counts.size):
+            seg = srt[offs[u]:offs[u + 1]]
+            assert np.array_equal(np.sort(seg), np.arange(offs[u], offs[u + 1])), (s, u)
+        st = g.read()
+        assert all(np.isfinite(st[k]).all() for k in KEYS), s
+    g.close()
+
+
 def test_massless_tracers_match_oracle():
     """A quarter of the bodies carry no mass (tracers).  Cells holding only tracers have no
     defined centre of mass (0/0, as in the reference's summarize), never pass the opening

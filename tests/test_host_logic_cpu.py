@@ -50,3 +50,20 @@ def test_workload_shapes():
     assert counts is None and arrs[0].size == 1000
     r = np.sqrt(arrs[0] ** 2 + arrs[1] ** 2 + arrs[2] ** 2)
     assert r.max() <= 1.0 + 1e-6
+
+
+def test_p99_ratio_interval_of_paired_errors():
+    """The bootstrap interval of the learned-over-plain p99 ratio: identical arms give
+    exactly 1; an arm scaled by 0.9 gives exactly 0.9 (every resample scales alike); and the
+    interval of two unrelated arms holds their point ratio."""
+    import numpy as np
+    import bench
+    rng = np.random.default_rng(3)
+    ep = rng.lognormal(-7.0, 1.0, size=(8, 4096))
+    assert bench._p99_ratio_interval(ep, ep, np) == [1.0, 1.0]
+    lo, hi = bench._p99_ratio_interval(0.9 * ep, ep, np)
+    assert abs(lo - 0.9) < 1e-12 and abs(hi - 0.9) < 1e-12
+    el = rng.lognormal(-7.1, 0.9, size=(8, 4096))
+    point = np.percentile(el, 99, axis=1).mean() / np.percentile(ep, 99, axis=1).mean()
+    lo, hi = bench._p99_ratio_interval(el, ep, np)
+    assert lo < point < hi and hi - lo < 0.2
