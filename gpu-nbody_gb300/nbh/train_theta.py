@@ -113,7 +113,7 @@ def study(n=1 << 20, seed=2024, grid=(0.4, 0.45, 0.5, 0.55, 0.6, 0.7, 0.8, 0.9, 
     return out
 
 
-FLOORS = (0.36, 0.4)
+FLOORS = (0.36, 0.4, 0.42, 0.45, 0.48)
 EVERY = (8,)              # steps between evaluations of the model
 TAU_FRACS = (0.5, 0.55, 0.6, 0.65)
 QUANTILES = (0.1,)
