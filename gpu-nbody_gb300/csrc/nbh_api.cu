@@ -54,7 +54,9 @@ struct nbh_sim {
     bool build_buckets = true;     // lock phases insert a sample, the rest is built per slot
     int top_phase = 0;             // config: where the first phase may build in shared memory
     bool top_possible = false;     // the loaded universes are small enough for it
-    bool top_build = false;        // in use (from top_phase and the universes, or the tuner's choice)
+    int top_cells = 0;             // cells of each block's shared tree for these universes
+    int top_split = 0;             // in use: 0 global locks, 1 or 8 shared-memory blocks per universe
+                                   // (from top_phase and the universes, or the tuner's choice)
     int4* buckets = nullptr;       // bucketed build: nbody records
     int* bwork = nullptr;          // bucketed build: 2 * nbody entries
     unsigned char* bstack = nullptr;   // bucketed build: per-warp task stacks
@@ -223,7 +225,8 @@ void enqueue_step(nbh_sim* sim, bool timed, cudaEvent_t vel_acc_ready = nullptr,
     if (timed) cudaEventRecord(sim->ev[0], s);
     launch_bbox(p, sim->grid_bbox, s);
     if (timed) cudaEventRecord(sim->ev[1], s);
-    launch_build(p, sim->build_phases, sim->build_buckets, sim->sms, sim->top_build, s);
+    launch_build(p, sim->build_phases, sim->build_buckets, sim->sms, sim->top_split ? sim->top_cells : 0,
+                 sim->top_split, s);
     launch_link(p, sim->grid_sum, s);
     if (timed) cudaEventRecord(sim->ev[2], s);
     launch_summarize(p, ref, sim->grid_sum, s);
@@ -259,7 +262,8 @@ void enqueue_tree(nbh_sim* sim, const StepParams& p) {
     const bool ref = sim->cfg.arith == NBH_ARITH_REFERENCE;
     cudaStream_t s = sim->stream;
     launch_bbox(p, sim->grid_bbox, s);
-    launch_build(p, sim->build_phases, sim->build_buckets, sim->sms, sim->top_build, s);
+    launch_build(p, sim->build_phases, sim->build_buckets, sim->sms, sim->top_split ? sim->top_cells : 0,
+                 sim->top_split, s);
     launch_link(p, sim->grid_sum, s);
     launch_summarize(p, ref, sim->grid_sum, s);
     launch_sort(p, sim->grid_sort, s);
@@ -548,7 +552,7 @@ int nbh_create(const nbh_config* cfg_in, nbh_sim** out) {
                                               "in [64, 256]");
     if (cfg.build_phases != 0 && cfg.build_phases != 1 && cfg.build_phases != 3 && cfg.build_phases != 5)
         return fail(nullptr, NBH_ERR_INVALID, "build_phases must be 1, 3 or 5");
-    if (cfg.top_phase < 0 || cfg.top_phase > 2) return fail(nullptr, NBH_ERR_INVALID, "top_phase must be 0, 1 or 2");
+    if (cfg.top_phase < 0 || cfg.top_phase > 3) return fail(nullptr, NBH_ERR_INVALID, "top_phase must be 0 to 3");
     if (cfg.build_buckets < 0 || cfg.build_buckets > 2)
         return fail(nullptr, NBH_ERR_INVALID, "build_buckets must be 0 (default), 1 (on) or 2 (off)");
     int ndev = 0;
@@ -646,12 +650,17 @@ int nbh_load_batch(nbh_sim* sim, int32_t nuniv, const int32_t* counts, const flo
     const int nw32 = (int)warps.size();
     int max_chunks = 0;          // chunks of the largest universe: the first phase's sample size
     for (int u = 0; u < nuniv; ++u) max_chunks = std::max(max_chunks, (counts[u] + 255) / 256);
-    // the default keeps the shared-memory first phase to universes of at most 2048 chunks:
-    // measured, it was 3 % faster on 256 universes of 1K-64K bodies (<= 256 chunks each),
-    // even on a 1M-body sphere (4096 chunks) and 15 % slower on a 4M-body disc (16384 chunks),
-    // whose sample is too much work for one block
+    // the default follows the measured build times: one shared-memory block per universe for
+    // universes of at most 512 chunks (256 universes of 1K-64K bodies: 3 % faster than the
+    // global first phase, eight blocks 2 % slower), eight for up to 8192 chunks (a 1M-body
+    // sphere, 4096 chunks: 3 % faster; one block: even), the global locks above (a 4M-body
+    // disc, 16384 chunks: 11-15 % slower in shared memory)
     sim->top_possible = max_chunks <= top_build_max_samples();
-    sim->top_build = sim->top_phase == 1 ? sim->top_possible : (sim->top_phase == 0 && max_chunks <= 2048);
+    sim->top_cells = top_build_cells(max_chunks);
+    if (!sim->top_possible || sim->top_phase == 2) sim->top_split = 0;
+    else if (sim->top_phase == 1) sim->top_split = 1;
+    else if (sim->top_phase == 3) sim->top_split = 8;
+    else sim->top_split = max_chunks <= 512 ? 1 : (max_chunks <= 8192 ? 8 : 0);
     for (int u = 0; u < nuniv; ++u)
         for (int s = sim->h_ubody[u]; s < sim->h_ubody[u + 1]; s += 64) warps.push_back(make_int2(s, u));
     const int nw64 = (int)warps.size() - nw32;
@@ -1327,41 +1336,43 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
     // universes allow it) and through the global locks
     const int phases_before = sim->build_phases;
     const bool buckets_before = sim->build_buckets;
-    const bool top_before = sim->top_build;
+    const int top_before = sim->top_split;
     const bool top_ok = sim->top_phase != 2 && sim->top_possible;
     float best_tree = 1e30f;
     int best_ph = phases_before;
     bool best_bk = buckets_before;
-    bool best_top = top_before;
+    int best_top = top_before;
     struct TreeCand {
         float ms;
         int phases;
-        bool buckets, top;
+        bool buckets;
+        int top;
     };
     std::vector<TreeCand> tcands;
-    const int tree_c[9][3] = {{1, 0, 0}, {3, 0, 0}, {5, 0, 0}, {3, 1, 0}, {5, 1, 0},
-                              {3, 0, 1}, {5, 0, 1}, {3, 1, 1}, {5, 1, 1}};
+    const int tree_c[13][3] = {{1, 0, 0}, {3, 0, 0}, {5, 0, 0}, {3, 1, 0}, {5, 1, 0},
+                               {3, 0, 1}, {5, 0, 1}, {3, 1, 1}, {5, 1, 1},
+                               {3, 0, 8}, {5, 0, 8}, {3, 1, 8}, {5, 1, 8}};
     for (const auto& tc : tree_c) {
         if (err != cudaSuccess) break;
         if (tc[2] && !top_ok) continue;
         sim->build_phases = tc[0];
         sim->build_buckets = tc[1] != 0;
-        sim->top_build = tc[2] != 0;
+        sim->top_split = tc[2];
         StepParams p = step_params(sim);
         p.theta_body = nullptr;
         float ms = 0.0f;
         err = timed([&] { enqueue_tree(sim, p); }, &ms);
         if (err != cudaSuccess) break;
         add_trial(1, tc[0], tc[1], tc[2], ms);
-        tcands.push_back({ms, tc[0], tc[1] != 0, tc[2] != 0});
+        tcands.push_back({ms, tc[0], tc[1] != 0, tc[2]});
         if (tc[0] == phases_before && (tc[1] != 0) == (buckets_before && phases_before != 1) &&
-            (tc[2] != 0) == (top_before && phases_before != 1))
+            tc[2] == (phases_before != 1 ? top_before : 0))
             out->ms_tree_before = ms;
         if (ms < best_tree) {
             best_tree = ms;
             best_ph = tc[0];
             best_bk = tc[1] != 0;
-            best_top = tc[2] != 0;
+            best_top = tc[2];
         }
     }
     if (err == cudaSuccess && tcands.size() > 1) {
@@ -1373,7 +1384,7 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
             launches.push_back([=] {
                 sim->build_phases = c.phases;
                 sim->build_buckets = c.buckets;
-                sim->top_build = c.top;
+                sim->top_split = c.top;
                 StepParams p = step_params(sim);
                 p.theta_body = nullptr;
                 enqueue_tree(sim, p);
@@ -1391,7 +1402,7 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
     cudaEventDestroy(b);
     sim->build_phases = phases_before;
     sim->build_buckets = buckets_before;
-    sim->top_build = top_before;
+    sim->top_split = top_before;
     if (err != cudaSuccess) return cuda_fail(sim, "nbh_autotune", err);
     CK(cudaMemcpyAsync(sim->h_state, sim->st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -1408,7 +1419,7 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
     sim->cfg.vote_width = best_v;
     sim->build_phases = best_ph;
     sim->build_buckets = best_bk;
-    sim->top_build = best_top;
+    sim->top_split = best_top;
     if ((e = set_geometry(sim))) return e;
     drop_graph(sim);
     out->force_threads = best_t;
@@ -1416,7 +1427,7 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
     out->stack_cap = best_c;
     out->build_phases = best_ph;
     out->build_buckets = best_bk ? 1 : 2;
-    out->top_phase = best_top ? 1 : 2;
+    out->top_phase = best_top == 8 ? 3 : (best_top == 1 ? 1 : 2);
     out->ms_force = best_ms;
     out->ms_tree = best_tree;
     return NBH_OK;

@@ -10,10 +10,12 @@ void launch_bbox(const StepParams& p, int grid, cudaStream_t s);
 // 1, 3 or 5 lock insertion phases; with `buckets` the lock phases (5: three of them; 3: one,
 // of 1/256) insert the sample and the rest is built as lock-free subtrees, one per slot of
 // the tree so far (3: two such passes, the first completing the 1/16 sample)
-// top: the first phase of a multi-phase schedule builds in shared memory, one block per
-// universe (when every universe has at most top_build_max_samples() chunks)
-void launch_build(const StepParams& p, int phases, bool buckets, int sms, bool top, cudaStream_t s);
+// top > 0: the first phase of a multi-phase schedule builds in shared memory, `split` (1 or
+// 8) blocks per universe holding `top` cells each (for universes of at most
+// top_build_max_samples() chunks; top_build_cells() sizes it); 0: through the global locks
+void launch_build(const StepParams& p, int phases, bool buckets, int sms, int top, int split, cudaStream_t s);
 int top_build_max_samples();
+int top_build_cells(int max_chunks);
 cudaError_t prepare_tree_kernels();   // raises the dynamic shared-memory limit of the top builder
 size_t bucket_stack_bytes(int sms);   // global task stacks of the bucketed build's grid
 void launch_link(const StepParams& p, int grid, cudaStream_t s);

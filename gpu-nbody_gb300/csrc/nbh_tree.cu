@@ -319,45 +319,55 @@ __global__ void __launch_bounds__(256) build_kernel(StepParams p, BuildPhase pha
 // The first insertion phase (one body of every 256-body chunk) in shared memory.  On an
 // empty tree that phase is the slowest one: every sampled body of a universe descends into
 // the same few top slots at once and waits on each split there in turn, through global
-// locks and release fences.  Here one block per universe builds those top levels in its
-// shared memory instead -- the same descents, the same centre arithmetic and the same CAS
-// locks, but on shared slots, where a lock round trip takes tens of cycles -- and then
-// publishes them: the new cells are taken from the pool with one atomic and every slot is
-// written once with its final value.  The tree is the one the global phase builds (an
-// octree does not depend on insertion order).  Cells are numbered in the order they are
-// made, and every cell is made after its parent, so the pool indices stay below their
-// parents'.  If the sample needs more cells than the block holds, or a split goes deeper
-// than the depth limit, the block inserts its sample through the global locks instead.
+// locks and release fences.  Here one block per universe, or eight (one per octant of the
+// root: more parallelism for a large sample, more blocks for many small ones), build those
+// top levels in their shared memory instead -- the same descents, the same centre
+// arithmetic and the same CAS locks, but on shared slots, where a lock round trip takes tens
+// of cycles -- and then publish them: each block takes its new cells from the pool with one
+// atomic, writes every slot once with its final value, and writes its root slots.  The tree is the one the global phase builds (an octree does not depend on
+// insertion order).  Cells are numbered in the order they are made, and every cell is made
+// after its parent, so the pool indices stay below their parents'.  If a block's sample
+// needs more cells than it holds, or a split goes deeper than the depth limit, that block
+// inserts its octant's sample through the global locks instead.
 //
 // Shared slots hold 16-bit values: a local cell (kTopCell | index), a sample (its index
 // within the universe's chunks), kTopNull or kTopLock.  Every slot is emptied before the
 // first descent, so a slot read before the write that fills it can only show kTopNull, and
 // acting on that goes through the CAS, which fails and returns the current value.
 constexpr int kTopThreads = 1024;
-constexpr int kTopCells = 12288;
+constexpr int kTopCells = 12288;               // largest shared tree of one block
 constexpr unsigned short kTopNull = 0xffffu, kTopLock = 0xfffeu, kTopCell = 0x8000u;
 constexpr BuildPhase kFirstPhase = {256, 0};
 constexpr long long kTopSpin = 1ll << 22;     // polls of a locked shared slot before giving up
 
 constexpr int kTopMaxSamples = 0x7ffe;       // sample indices stay below kTopLock and kTopCell
 int top_build_max_samples() { return kTopMaxSamples; }
-size_t top_build_smem() { return (size_t)kTopCells * 8 * sizeof(unsigned short) + kTopCells; }
+// Cells a block's shared tree holds for universes of at most max_chunks chunks: an octree of
+// k bodies has about k/2 cells, and a block holds one octant's share; chains of single-child
+// cells between close pairs take more, and a block that runs out falls back.
+int top_build_cells(int max_chunks) {
+    const int want = ((max_chunks + 64) + 63) / 64 * 64;
+    return want < kTopCells ? want : kTopCells;
+}
+static size_t top_build_smem(int cells) { return (size_t)cells * 8 * sizeof(unsigned short) + cells; }
 
 __device__ __forceinline__ unsigned short ld_shared_volatile(const unsigned short* a) {
     return *reinterpret_cast<const volatile unsigned short*>(a);
 }
 
-__global__ void __launch_bounds__(kTopThreads) top_build_kernel(StepParams p, bool zero_counts) {
+__global__ void __launch_bounds__(kTopThreads) top_build_kernel(StepParams p, bool zero_counts, int cap,
+                                                                 int split) {
     extern __shared__ __align__(16) unsigned char top_smem[];
-    unsigned short* slots = reinterpret_cast<unsigned short*>(top_smem);          // [kTopCells][8]
-    unsigned char* lvl = top_smem + (size_t)kTopCells * 8 * sizeof(unsigned short);
+    unsigned short* slots = reinterpret_cast<unsigned short*>(top_smem);          // [cap][8]
+    unsigned char* lvl = top_smem + (size_t)cap * 8 * sizeof(unsigned short);
     __shared__ int ncell, failed, c0, gbase, depth_max, status;
     // one read of the status word for the whole block: threads that saw different values
     // would part at the barriers below
     if (threadIdx.x == 0) status = load_status(p.st);
     __syncthreads();
     if (status) return;
-    const int u = blockIdx.x;
+    const int u = split == 8 ? (int)(blockIdx.x >> 3) : (int)blockIdx.x;   // universe
+    const int oct = split == 8 ? (int)(blockIdx.x & 7) : -1;   // this block's octant of the root (-1: all)
     const int nbody = p.nbody;
     const int nsamp = (p.ubody[u + 1] - p.ubody[u] + 255) / 256;    // chunks of universe u
     if (threadIdx.x == 0) {
@@ -373,7 +383,7 @@ __global__ void __launch_bounds__(kTopThreads) top_build_kernel(StepParams p, bo
         depth_max = 1;
         lvl[0] = 0;
     }
-    for (int i = threadIdx.x; i < kTopCells * 4; i += blockDim.x) reinterpret_cast<unsigned*>(slots)[i] = 0xffffffffu;
+    for (int i = threadIdx.x; i < cap * 4; i += blockDim.x) reinterpret_cast<unsigned*>(slots)[i] = 0xffffffffu;
     __syncthreads();
     const int root = p.nnodes - u;
     const float4 rc = p.node4[root];
@@ -389,6 +399,7 @@ __global__ void __launch_bounds__(kTopThreads) top_build_kernel(StepParams p, bo
             int node = 0, depth = 1;
             float r = radius, cx = rc.x, cy = rc.y, cz = rc.z;
             int path = octant(cx, cy, cz, bp.x, bp.y, bp.z);
+            if (oct >= 0 && path != oct) continue;     // another block's octant
             unsigned short* slot = slots + node * 8 + path;
             unsigned short ch = ld_shared_volatile(slot);
             bool done = false;
@@ -440,7 +451,7 @@ __global__ void __launch_bounds__(kTopThreads) top_build_kernel(StepParams p, bo
                 for (;;) {
                     ++depth;
                     const int cell = atomicAdd(&ncell, 1);
-                    if (depth > kMaxDepth || cell >= kTopCells) {
+                    if (depth > kMaxDepth || cell >= cap) {
                         atomicExch(&failed, 1);
                         ok = false;
                         break;
@@ -476,11 +487,15 @@ __global__ void __launch_bounds__(kTopThreads) top_build_kernel(StepParams p, bo
     if (failed) {
         // more cells than the block holds, or a very deep split: the global lock insertion
         int lm = 1, waits = 0, misses = 0;
+        const float4 rc0 = p.node4[root];
         for (int smp = threadIdx.x; smp < nsamp; smp += blockDim.x) {
             const long long ci = c0 + smp;
             const int4 ck = p.chunks[ci];
             const int b = ck.y + phase_offset(kFirstPhase, 0, ci);
-            if (b < ck.z && !lock_insert(p, b, u, zero_counts, lm, waits, misses)) break;
+            if (b >= ck.z) continue;
+            const float4 bp = p.node4[b];
+            if (oct >= 0 && octant(rc0.x, rc0.y, rc0.z, bp.x, bp.y, bp.z) != oct) continue;   // another block's
+            if (!lock_insert(p, b, u, zero_counts, lm, waits, misses)) break;
         }
         if (lm > ld_relaxed(&p.st->max_depth)) atomicMax(&p.st->max_depth, lm);
         if (waits) atomicAdd(&p.st->lock_waits[blockIdx.x % kDiagSlots], waits);
@@ -503,6 +518,7 @@ __global__ void __launch_bounds__(kTopThreads) top_build_kernel(StepParams p, bo
     const int gb = gbase;
     for (int i = threadIdx.x; i < nc * 8; i += blockDim.x) {
         const int c = i >> 3;
+        if (c == 0 && oct >= 0 && (i & 7) != oct) continue;   // the root's other slots are other blocks'
         const unsigned short v = slots[i];
         int g = kNull;
         if (v != kTopNull) {
@@ -1238,20 +1254,21 @@ static void launch_bucket_pass(const StepParams& p, BuildPhase set, bool first, 
 
 // The first phase (one body per chunk) of the multi-phase schedules: in shared memory (one
 // block per universe) when `top`, else through the global locks.
-static void launch_first_phase(const StepParams& p, bool zero_counts, bool top, cudaStream_t s) {
-    if (top)
-        top_build_kernel<<<p.nuniv, kTopThreads, top_build_smem(), s>>>(p, zero_counts);
+static void launch_first_phase(const StepParams& p, bool zero_counts, int top_cells, int split, cudaStream_t s) {
+    if (top_cells > 0)
+        top_build_kernel<<<split * p.nuniv, kTopThreads, top_build_smem(top_cells), s>>>(p, zero_counts, top_cells,
+                                                                                       split);
     else
         build_kernel<<<(unsigned)((p.nchunks * (long long)phase_bodies(kFirstPhase) + 255) / 256), 256, 0, s>>>(
             p, kFirstPhase, zero_counts);
 }
 
-void launch_build(const StepParams& p, int phases, bool buckets, int sms, bool top, cudaStream_t s) {
+void launch_build(const StepParams& p, int phases, bool buckets, int sms, int top, int split, cudaStream_t s) {
     buckets = buckets && phases != 1;
     if (buckets && phases == 3) {
         // one lock phase (1/256 of each chunk), then the rest of the 1/16 sample as bucket
         // subtrees of that tree, then every other body as bucket subtrees of the sample's
-        launch_first_phase(p, true, top, s);
+        launch_first_phase(p, true, top, split, s);
         launch_bucket_pass(p, kThreePhases[1], true, true, sms, s);
         launch_bucket_pass(p, kBucketBodies, false, false, sms, s);
         return;
@@ -1261,7 +1278,7 @@ void launch_build(const StepParams& p, int phases, bool buckets, int sms, bool t
     if (buckets) count -= 2;   // five phases: the lock phases insert the 1/16 sample only
     for (int k = 0; k < count; ++k) {
         if (k == 0 && phases != 1) {
-            launch_first_phase(p, buckets, top, s);
+            launch_first_phase(p, buckets, top, split, s);
             continue;
         }
         const long long bodies = (long long)p.nchunks * phase_bodies(sched[k]);
@@ -1271,7 +1288,8 @@ void launch_build(const StepParams& p, int phases, bool buckets, int sms, bool t
 }
 
 cudaError_t prepare_tree_kernels() {
-    return cudaFuncSetAttribute(top_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)top_build_smem());
+    return cudaFuncSetAttribute(top_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)top_build_smem(kTopCells));
 }
 
 size_t bucket_stack_bytes(int sms) {

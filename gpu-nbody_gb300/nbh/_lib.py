@@ -71,7 +71,7 @@ class NbhDiag(C.Structure):
 
 NBH_DIAG_POTENTIAL = 1
 NBH_TUNE_VOTE = 1
-NBH_TUNE_MAX_TRIALS = 48
+NBH_TUNE_MAX_TRIALS = 64
 
 
 class NbhTune(C.Structure):

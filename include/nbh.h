@@ -97,13 +97,13 @@ typedef struct nbh_config {
                               phase inserts 1/256 and two such passes add the rest of the
                               sample, then the other bodies; 2: lock insertion only */
     int32_t top_phase;     /* the first phase of a 3- or 5-phase schedule (one body of every
-                              256) builds the top levels of each universe's tree in shared
-                              memory, one block per universe, and publishes them (the same
-                              tree): 0 (default) where every universe has at most 2048 * 256
-                              bodies (many small universes: faster; one large universe: one
-                              block is too little parallelism), 1 wherever every universe has
-                              at most 32766 * 256 bodies, 2 never (global locks);
-                              nbh_autotune times both where possible */
+                              256) may build the top levels of each universe's tree in shared
+                              memory and publish them (the same tree), for universes of at
+                              most 32766 * 256 bodies: 1 with one block per universe, 3 with
+                              eight (one per octant of the root), 2 never (global locks);
+                              0 (default): one block up to 512 * 256 bodies per universe,
+                              eight up to 8192 * 256, the global locks above (the measured
+                              fastest); nbh_autotune times all three where possible */
     int32_t reserved[3];
 } nbh_config;
 
@@ -273,7 +273,7 @@ int nbh_diagnostics(nbh_sim* sim, int32_t flags, nbh_diag* out, int32_t nout);
  * larger group opens a few more cells), so it is off unless asked for.  Body state and the
  * step counter are left as they were. */
 #define NBH_TUNE_VOTE 1
-#define NBH_TUNE_MAX_TRIALS 48
+#define NBH_TUNE_MAX_TRIALS 64
 typedef struct nbh_tune {
     int32_t force_threads;         /* chosen */
     int32_t stack_cap;             /* chosen */
@@ -289,10 +289,12 @@ typedef struct nbh_tune {
     int32_t trial_kind[NBH_TUNE_MAX_TRIALS];    /* 0 force, 1 tree */
     int32_t trial_a[NBH_TUNE_MAX_TRIALS];       /* threads, or insertion phases */
     int32_t trial_b[NBH_TUNE_MAX_TRIALS];       /* stack capacity (force), or bucketed (tree) */
-    int32_t trial_vote[NBH_TUNE_MAX_TRIALS];    /* vote width (force), or 1 when the first phase
-                                                   built in shared memory (tree) */
+    int32_t trial_vote[NBH_TUNE_MAX_TRIALS];    /* vote width (force); blocks per universe of
+                                                   the shared-memory first phase, 0 for the
+                                                   global locks (tree) */
     float   trial_ms[NBH_TUNE_MAX_TRIALS];      /* mean of 3 timed launches after 1 warm-up */
-    int32_t top_phase;             /* chosen: 1 first phase in shared memory, 2 global locks */
+    int32_t top_phase;             /* chosen first phase, as nbh_config.top_phase: 1 or 3
+                                      shared memory (one or eight blocks per universe), 2 global */
 } nbh_tune;
 int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out);
 

@@ -116,14 +116,17 @@ def test_fma_mode_ten_steps_positions():
         assert np.abs(gs[k] - os_[k]).max() <= 1e-5 * scale, k
 
 
-@pytest.mark.parametrize("phases,buckets,top", [(5, 1, 0), (3, 1, 0), (5, 2, 0), (1, 2, 0), (5, 1, 2), (3, 2, 2)],
+@pytest.mark.parametrize("phases,buckets,top", [(5, 1, 0), (3, 1, 0), (5, 2, 0), (1, 2, 0), (5, 1, 2), (3, 2, 2),
+                                               (5, 1, 3), (3, 2, 3)],
                          ids=["five-bucketed", "two-pass-bucketed", "five-lock", "one-pass",
-                              "five-bucketed-global-first-phase", "three-lock-global-first-phase"])
+                              "five-bucketed-global-first-phase", "three-lock-global-first-phase",
+                              "five-bucketed-eight-blocks", "three-lock-eight-blocks"])
 def test_tree_matches_oracle_and_invariants(phases, buckets, top):
     """Same octree as the oracle (slot by slot), every body in exactly one slot, body
     counts add up, root mass = total mass, centres of mass equal the oracle's bit for bit
     (same summation order) -- under every build schedule, with the first phase built in
-    shared memory (the default) or through the global locks."""
+    shared memory (one block per universe, the default at this size, or eight) or through the
+    global locks."""
     n = 20000
     arrs = plummer(n, seed=9)
     g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=32, build_phases=phases, build_buckets=buckets,
@@ -168,7 +171,8 @@ def test_rebuilds_under_contention_hold_every_body_and_repeat():
     """1M-body Plummer sphere with dt = 0: every step rebuilds the same octree from the same
     positions.  Under every build schedule (one lock pass: all bodies contend at once; five
     lock phases; five phases with the bucketed completion; one lock phase with two bucketed
-    passes; five bucketed phases with the first phase in shared memory) each rebuild reaches every body
+    passes; five bucketed phases with the first phase in one shared-memory block instead of
+    the eight the default takes at this size) each rebuild reaches every body
     exactly once from the root, counts them all, and gives the same depth-first order and
     the same accelerations, bit for bit, as every other rebuild and schedule.  (Summarize
     used to decide from a cell's slots while the cell's own compaction rewrote them; in up to
@@ -201,24 +205,26 @@ def test_rebuilds_under_contention_hold_every_body_and_repeat():
 
 def test_first_phase_falls_back_to_global_locks_when_shared_memory_is_full():
     """The first insertion phase (one body of every 256-body chunk) builds the top of the tree
-    in shared memory, which holds 12,288 cells.  Here the 2,048 sampled bodies come in close
-    pairs (2^-17 of the extent apart), so each pair makes a chain of ~15 single-child cells and
-    the sample needs more cells than that: the block inserts its sample through the global
-    locks instead.  The tree equals the oracle's slot by slot, and the step equals the one
-    with the global first phase chosen from the start, bit for bit."""
+    in shared memory, one block per universe or one per octant of the root, each holding about
+    one cell per sampled body of the universe (2,112 here).  Here all 2,048 sampled bodies lie
+    in one octant and come in close pairs (2^-17 of the extent apart), so each pair makes a
+    chain of ~15 single-child cells and that octant needs ~13,700 cells: the block inserts its
+    sample through the global locks instead, in both layouts.  The tree equals the oracle's slot by slot, and the
+    step equals the one with the global first phase chosen from the start, bit for bit."""
     n = 2048 * 256
     rng = np.random.default_rng(11)
     x, y, z = (rng.uniform(-1.0, 1.0, n).astype(np.float32) for _ in range(3))
     m = np.full(n, 1.0 / n, np.float32)
     chunk = np.arange(n // 256)
     smp = chunk * 256 + ((7 * chunk) & 15)          # the first phase's body of each chunk
+    x[smp], y[smp], z[smp] = np.abs(x[smp]), np.abs(y[smp]), np.abs(z[smp])   # one octant
     d = np.float32(2.0 ** -17)
     for k in range(0, smp.size, 2):                 # every second sample sits next to the one before
         a, b = smp[k], smp[k + 1]
         x[b], y[b], z[b] = x[a] + d, y[a], z[a]
     arrs = (x, y, z, None, None, None, m)
     outs = []
-    for top in (0, 2):
+    for top in (1, 3, 2):
         g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=64, top_phase=top)
         g.load(*arrs)
         g.step()
@@ -231,10 +237,11 @@ def test_first_phase_falls_back_to_global_locks_when_shared_memory_is_full():
     gt, ot = outs[0][0], o.tree_arrays()
     assert assert_same_tree(gt, ot, n, gt["nnodes"], o.nn) == gt["nnodes"] + 1 - gt["bottom"]
     np.testing.assert_array_equal(gt["sorted"], ot["sorted"])
-    np.testing.assert_array_equal(gt["sorted"], outs[1][0]["sorted"])
-    assert outs[0][2] == outs[1][2]
-    for k in KEYS:
-        np.testing.assert_array_equal(outs[0][1][k], outs[1][1][k])
+    for other in outs[1:]:
+        np.testing.assert_array_equal(gt["sorted"], other[0]["sorted"])
+        assert outs[0][2] == other[2]
+        for k in KEYS:
+            np.testing.assert_array_equal(outs[0][1][k], other[1][k])
 
 
 def test_batch_of_universes_matches_oracle_per_universe():
