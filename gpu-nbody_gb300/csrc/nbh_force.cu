@@ -468,12 +468,23 @@ __global__ void __launch_bounds__(kOrderThreads) item_order_kernel(const int* __
     const unsigned lt = (1u << lane) - 1u;
     if (threadIdx.x < kOrderClasses) cnt[threadIdx.x] = 0;
     __syncthreads();
-    for (int i0 = 0; i0 < nitems; i0 += blockDim.x) {
-        const int i = i0 + threadIdx.x;
-        const bool v = i < nitems;
-        const int cls = v ? cost_class(cost[i]) : -1;
-        const unsigned grp = __match_any_sync(0xffffffffu, cls);
-        if (v && lane == __ffs(grp) - 1) atomicAdd(&cnt[cls], __popc(grp));
+    // four items per thread per round: their cost loads are in flight together
+    constexpr int kU = 4;
+    const int stride = blockDim.x;
+    for (int i0 = 0; i0 < nitems; i0 += kU * stride) {
+        int c[kU];
+#pragma unroll
+        for (int k = 0; k < kU; ++k) {
+            const int i = i0 + k * stride + threadIdx.x;
+            c[k] = i < nitems ? cost[i] : -1;
+        }
+#pragma unroll
+        for (int k = 0; k < kU; ++k) {
+            const bool v = c[k] >= 0;
+            const int cls = v ? cost_class(c[k]) : -1;
+            const unsigned grp = __match_any_sync(0xffffffffu, cls);
+            if (v && lane == __ffs(grp) - 1) atomicAdd(&cnt[cls], __popc(grp));
+        }
     }
     __syncthreads();
     if (threadIdx.x < 32) {
@@ -496,16 +507,25 @@ __global__ void __launch_bounds__(kOrderThreads) item_order_kernel(const int* __
         off[c0 - 3] = base + n0 + n1 + n2;
     }
     __syncthreads();
-    for (int i0 = 0; i0 < nitems; i0 += blockDim.x) {
-        const int i = i0 + threadIdx.x;
-        const bool v = i < nitems;
-        const int cls = v ? cost_class(cost[i]) : -1;
-        const unsigned grp = __match_any_sync(0xffffffffu, cls);
-        const int leader = __ffs(grp) - 1;
-        int base = 0;
-        if (v && lane == leader) base = atomicAdd(&off[cls], __popc(grp));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (v) order[base + __popc(grp & lt)] = i;
+    for (int i0 = 0; i0 < nitems; i0 += kU * stride) {
+        int c[kU];
+#pragma unroll
+        for (int k = 0; k < kU; ++k) {
+            const int i = i0 + k * stride + threadIdx.x;
+            c[k] = i < nitems ? cost[i] : -1;
+        }
+#pragma unroll
+        for (int k = 0; k < kU; ++k) {
+            const int i = i0 + k * stride + threadIdx.x;
+            const bool v = c[k] >= 0;
+            const int cls = v ? cost_class(c[k]) : -1;
+            const unsigned grp = __match_any_sync(0xffffffffu, cls);
+            const int leader = __ffs(grp) - 1;
+            int base = 0;
+            if (v && lane == leader) base = atomicAdd(&off[cls], __popc(grp));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (v) order[base + __popc(grp & lt)] = i;
+        }
     }
 }
 
