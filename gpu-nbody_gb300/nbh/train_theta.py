@@ -115,9 +115,9 @@ def study(n=1 << 20, seed=2024, grid=(0.4, 0.45, 0.5, 0.55, 0.6, 0.7, 0.8, 0.9, 
 
 FLOORS = (0.36, 0.4, 0.42, 0.45, 0.48)
 EVERY = (8,)              # steps between evaluations of the model
-TAU_FRACS = (0.5, 0.55, 0.6, 0.65)
+TAU_FRACS = (0.55, 0.6, 0.65)
 QUANTILES = (0.1,)
-INIT_SEEDS = (0, 1)       # initial weights of the network
+INIT_SEEDS = (0, 1, 2)    # initial weights of the network
 VAL_SEEDS = (103, 104, 105)   # held-out Plummer spheres of the selection
 # the p99 of one realisation moves by several per cent from sphere to sphere at the same
 # settings: a candidate's p99 ratio, averaged over the held-out spheres, must stay within
