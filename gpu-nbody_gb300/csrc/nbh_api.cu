@@ -50,6 +50,7 @@ struct nbh_sim {
     int theta_group = 0;           // 1: each vote group walks with its smallest angle
     int force_threads = 128;       // force launch geometry (nbh_autotune)
     int stack_cap = 256;
+    bool force_list = true;        // 64-wide walks without features: the lane-parallel list walk
     int build_phases = 5;          // octree insertion launches
     bool build_buckets = true;     // lock phases insert a sample, the rest is built per slot
     int top_phase = 0;             // config: where the first phase may build in shared memory
@@ -172,6 +173,7 @@ StepParams step_params(const nbh_sim* sim) {
     p.theta_body = sim->theta_active ? sim->theta_body : nullptr;
     p.theta_group = sim->theta_group;
     p.stack_cap = sim->stack_cap;
+    p.force_list = sim->force_list ? 1 : 0;
     p.buckets = sim->buckets;
     p.bwork = sim->bwork;
     p.bstack = sim->bstack;
@@ -298,7 +300,7 @@ int set_geometry(nbh_sim* sim) {
     int occ_sort = 0, occ_force = 0;
     CK(static_cast<cudaError_t>(occupancy_sort(&occ_sort)));
     CK(static_cast<cudaError_t>(occupancy_force(sim->cfg.vote_width, sim->cfg.arith == NBH_ARITH_REFERENCE,
-                                                sim->force_threads, sim->stack_cap, &occ_force)));
+                                                sim->force_threads, sim->stack_cap, sim->force_list, &occ_force)));
     sim->grid_bbox = std::max(1, std::min(sim->nchunks, 4 * sms));
     sim->grid_sum = std::max(1, (sim->nbody + 255) / 256);
     sim->grid_sort = std::max(1, std::min(occ_sort * sms, (sim->ncells + 255) / 256));
@@ -553,6 +555,8 @@ int nbh_create(const nbh_config* cfg_in, nbh_sim** out) {
     if (cfg.build_phases != 0 && cfg.build_phases != 1 && cfg.build_phases != 3 && cfg.build_phases != 5)
         return fail(nullptr, NBH_ERR_INVALID, "build_phases must be 1, 3 or 5");
     if (cfg.top_phase < 0 || cfg.top_phase > 3) return fail(nullptr, NBH_ERR_INVALID, "top_phase must be 0 to 3");
+    if (cfg.force_list < 0 || cfg.force_list > 2)
+        return fail(nullptr, NBH_ERR_INVALID, "force_list must be 0 (default), 1 (on) or 2 (off)");
     if (cfg.build_buckets < 0 || cfg.build_buckets > 2)
         return fail(nullptr, NBH_ERR_INVALID, "build_buckets must be 0 (default), 1 (on) or 2 (off)");
     int ndev = 0;
@@ -573,6 +577,8 @@ int nbh_create(const nbh_config* cfg_in, nbh_sim** out) {
     sim->build_phases = cfg.build_phases ? cfg.build_phases : 5;
     sim->build_buckets = cfg.build_buckets != 2;
     sim->top_phase = cfg.top_phase;
+    // precise mode keeps the reference's order of accumulation (the per-visit walk) unless asked
+    sim->force_list = cfg.force_list == 1 || (cfg.force_list == 0 && !cfg.precise);
     sim->sms = prop.multiProcessorCount;
     if ((e = cudaSetDevice(cfg.device)) != cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&sim->stream, cudaStreamNonBlocking)) != cudaSuccess ||
@@ -1282,8 +1288,14 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
     for (const auto& g : geo) {
         if (err != cudaSuccess) break;
         if (!force_geometry_valid(vote, g.first, g.second)) continue;
+        // the list walk's stack holds cells, and 256 of them are never slower: only block
+        // sizes are timed (and the geometry in place)
+        const bool in_place = g.first == sim->force_threads && g.second == sim->stack_cap;
+        if (vote == 64 && sim->force_list && g.second != 256 && !in_place) continue;
         int occ = 0;
-        if ((err = static_cast<cudaError_t>(occupancy_force(vote, ref, g.first, g.second, &occ))) != cudaSuccess) break;
+        if ((err = static_cast<cudaError_t>(occupancy_force(vote, ref, g.first, g.second, sim->force_list, &occ))) !=
+            cudaSuccess)
+            break;
         if (occ < 1) continue;
         StepParams q = step_params(sim);
         q.theta_body = nullptr;

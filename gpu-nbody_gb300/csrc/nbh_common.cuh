@@ -114,6 +114,7 @@ struct StepParams {
     int theta_group;     // per-body theta: 1 = each vote group walks with its smallest angle
     int feat_gate;       // force launch gated on the learned-theta schedule: 0 none,
                          // 1 run only on bound-recording steps, 2 only on the others
+    int force_list;      // 1: 64-wide walks without features take the lane-parallel list walk
 };
 
 __device__ __forceinline__ int* cell_child(const StepParams& p, int c) {

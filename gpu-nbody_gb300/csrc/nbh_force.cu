@@ -26,6 +26,15 @@ constexpr size_t force_smem_bytes(int threads, int cap) {
     return (size_t)(threads / group_lanes<W>()) * cap * (sizeof(float4) + sizeof(int2));
 }
 
+// The list walk (64-wide groups): per group, the records of accepted nodes awaiting
+// evaluation (at most 31 wait after an evaluation and one round adds at most 32) and a
+// stack of `cap` cells whose children are still to be tested, with their levels (a
+// 64-entry stack also holds the per-level walk's 2 * kMaxDepth ints).
+constexpr int kListCap = 64;
+constexpr size_t list_group_bytes(int cap) { return kListCap * sizeof(float4) + (size_t)cap * sizeof(int2); }
+constexpr size_t force_list_smem_bytes(int threads, int cap) { return (size_t)(threads / 32) * list_group_bytes(cap); }
+static_assert(kStackCapMin * sizeof(int2) >= 2 * kMaxDepth * sizeof(int), "the per-level walk fits the cell stack");
+
 // Opening threshold of tree level L (root = 0): r^2/theta^2 * 4^-L + eps^2
 // (calculateforce.cl:52-67).  The walk carries s = 4^-L (exact powers of two) and forms
 // t0*s + eps^2, which equals ldexp(t0, -2L) + eps^2 in the normal range; below it eps^2
@@ -67,6 +76,25 @@ __device__ __forceinline__ float dist2(const float dx, const float dy, const flo
         return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmaf_rn(dz, dz, eps2)));
 }
 
+// Evaluate the first cnt records of a group's list for the lane's bodies, in list order.
+template <int BPL>
+__device__ __forceinline__ void eval_list(const float4* lst, const int cnt, const float4 (&pb)[BPL],
+                                          const float eps2, float (&ax)[BPL], float (&ay)[BPL], float (&az)[BPL],
+                                          float (&eb)[BPL]) {
+#pragma unroll 4
+    for (int i = 0; i < cnt; ++i) {
+        const float4 q = lst[i];
+#pragma unroll
+        for (int k = 0; k < BPL; ++k) {
+            const float dx = __fsub_rn(q.x, pb[k].x);
+            const float dy = __fsub_rn(q.y, pb[k].y);
+            const float dz = __fsub_rn(q.z, pb[k].z);
+            const float d2 = dist2<false>(dx, dy, dz, eps2);
+            interact<false, false>(q, dx, dy, dz, d2, ax[k], ay[k], az[k], eb[k], 0.0f);
+        }
+    }
+}
+
 // -------------------------------------------------------------------------------------
 // Force (calculateforce.cl:52-185).  A group of W bodies (W = 32: one warp; W = 16: the
 // reference's work-group, :99,145; W = 64: one warp with two bodies per lane) takes W
@@ -97,8 +125,23 @@ __device__ __forceinline__ float dist2(const float dx, const float dy, const flo
 // results go to p.probe (x, y, z, bound) and no body state changes (force probe).  With
 // p.feat_gate set, a launch that does not match the step's place in the learned-theta
 // schedule returns at once (the step graph holds a recording and a plain launch).
-template <int W, bool REF, bool PB, bool FEAT>
+//
+// LIST (W = 64, FMA arithmetic, no features): the same votes, taken lane-parallel.  Each
+// round the lanes take the children of up to four cells from the group's cell stack, one
+// child per lane (8 lanes per cell), and decide each child on its own lane: a body is
+// accepted; a cell is accepted when even the group's bounding box passes the test (the
+// box's distance components bound every body's from below, and the rounded subtractions,
+// the fused squares and the comparison are monotone, so every body's own test passes), and
+// opened when the group's body nearest the box centre fails it (then the vote fails).  Only
+// the remaining cells take the vote of every body, one after another.  Accepted records go
+// to a list in shared memory, evaluated 32 to 63 at a time in a loop of arithmetic alone:
+// the same interactions as the per-visit walk, accumulated in list order (rounding may
+// differ from it in the last bits).  A cell stack that would overflow restarts the group
+// on the per-level walk (stack_cap entries: 256 by default, enough for every 64-body group
+// of the benchmarked spheres, which needed at most 99).
+template <int W, bool REF, bool PB, bool FEAT, bool LIST = false>
 __device__ __forceinline__ void force_walk(const StepParams& p) {
+    static_assert(!LIST || (W == 64 && !REF && !FEAT), "the list walk is the 64-wide FMA walk without features");
     if (load_status(p.st)) return;
     if (p.feat_gate && theta_bound_step(p.st, p.st->step) != (p.feat_gate == 1)) return;
     constexpr int GL = group_lanes<W>();            // lanes per group
@@ -117,7 +160,11 @@ __device__ __forceinline__ void force_walk(const StepParams& p) {
     const unsigned gmask = (GL == 32) ? 0xffffffffu : (0xffffu << (16 * (lane >> 4)));
     float4* const sq = sq_all + grp * cap;           // node record of each pending child
     int2* const se = se_all + grp * cap;             // (node index, bits of threshold or level factor)
-    int* const snode = reinterpret_cast<int*>(se);   // deep-tree walk: (cell, next) per level
+    // list walk: the group's list of accepted records and its stack of (cell, level)
+    float4* const lst = reinterpret_cast<float4*>(smem_raw + (size_t)grp * list_group_bytes(cap));
+    int2* const cst = reinterpret_cast<int2*>(lst + kListCap);
+    // deep-tree walk: (cell, next) per level
+    int* const snode = LIST ? reinterpret_cast<int*>(cst) : reinterpret_cast<int*>(se);
     int* const snext = snode + kMaxDepth;
     const int nbody = p.nbody;
     const float eps2 = p.eps2;
@@ -181,7 +228,156 @@ __device__ __forceinline__ void force_walk(const StepParams& p) {
         const int root = p.nnodes - u;
 
         if (gvalid) {
-            if (fast) {
+            bool walked = false;
+            if constexpr (LIST) {
+                walked = true;
+                // the group's bounding box (lanes past the end hold the first body)
+                float lox = fminf(pb[0].x, pb[1].x), loy = fminf(pb[0].y, pb[1].y), loz = fminf(pb[0].z, pb[1].z);
+                float hix = fmaxf(pb[0].x, pb[1].x), hiy = fmaxf(pb[0].y, pb[1].y), hiz = fmaxf(pb[0].z, pb[1].z);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    lox = fminf(lox, __shfl_xor_sync(0xffffffffu, lox, o));
+                    loy = fminf(loy, __shfl_xor_sync(0xffffffffu, loy, o));
+                    loz = fminf(loz, __shfl_xor_sync(0xffffffffu, loz, o));
+                    hix = fmaxf(hix, __shfl_xor_sync(0xffffffffu, hix, o));
+                    hiy = fmaxf(hiy, __shfl_xor_sync(0xffffffffu, hiy, o));
+                    hiz = fmaxf(hiz, __shfl_xor_sync(0xffffffffu, hiz, o));
+                }
+                // the representative: the body nearest the box centre (lowest index on ties)
+                const float cx = 0.5f * (lox + hix), cy = 0.5f * (loy + hiy), cz = 0.5f * (loz + hiz);
+                float best = 0.0f;
+                int bid = 0;
+#pragma unroll
+                for (int k = 0; k < BPL; ++k) {
+                    const float ex = pb[k].x - cx, ey = pb[k].y - cy, ez = pb[k].z - cz;
+                    const float d = ex * ex + ey * ey + ez * ez;
+                    if (k == 0 || d < best) {
+                        best = d;
+                        bid = lane * BPL + k;
+                    }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+                    const int oi = __shfl_xor_sync(0xffffffffu, bid, o);
+                    if (ob < best || (ob == best && oi < bid)) {
+                        best = ob;
+                        bid = oi;
+                    }
+                }
+                const int rsrc = bid / BPL, rk = bid % BPL;
+                float4 rp = pb[0];
+                float rt = t0[0];
+#pragma unroll
+                for (int k = 1; k < BPL; ++k)
+                    if (rk == k) {
+                        rp = pb[k];
+                        rt = t0[k];
+                    }
+                rp.x = __shfl_sync(0xffffffffu, rp.x, rsrc);
+                rp.y = __shfl_sync(0xffffffffu, rp.y, rsrc);
+                rp.z = __shfl_sync(0xffffffffu, rp.z, rsrc);
+                // thresholds: the box takes the group's largest r^2/theta^2 (the smallest angle)
+                float tlb = t0[0], trep = t0[0];
+                if constexpr (PB) {
+#pragma unroll
+                    for (int k = 1; k < BPL; ++k) tlb = fmaxf(tlb, t0[k]);
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) tlb = fmaxf(tlb, __shfl_xor_sync(0xffffffffu, tlb, o));
+                    trep = __shfl_sync(0xffffffffu, rt, rsrc);
+                }
+                const unsigned lt = (1u << lane) - 1u;
+                if (lane == 0) cst[0] = make_int2(root, 0);
+                int ctop = 1, lcnt = 0, tested = 0;
+                long long accepted = 0;
+                __syncwarp();
+                while (ctop > 0) {
+                    const int k4 = min(4, ctop);
+                    const int ci = lane >> 3;
+                    int chk = kNull, lv = 0;
+                    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (ci < k4) {
+                        const int2 e = cst[ctop - 1 - ci];
+                        lv = e.y;
+                        const size_t o8 = ((size_t)(e.x - nbody) << 3) + (lane & 7);
+                        chk = __ldg(child + o8);
+                        q = __ldg(kids4 + o8);
+                    }
+                    ctop -= k4;
+                    __syncwarp();          // the popped entries are read before pushes reuse them
+                    // children of a level-lv cell: t0 * 4^-lv + eps^2 (4^-lv exact)
+                    const float sl = __int_as_float((127 - 2 * lv) << 23);
+                    bool acc = chk >= 0 && chk < nbody;
+                    bool opn = false, inc = false;
+                    if (chk >= nbody) {
+                        const float gx = fmaxf(fmaxf(__fsub_rn(q.x, hix), __fsub_rn(lox, q.x)), 0.0f);
+                        const float gy = fmaxf(fmaxf(__fsub_rn(q.y, hiy), __fsub_rn(loy, q.y)), 0.0f);
+                        const float gz = fmaxf(fmaxf(__fsub_rn(q.z, hiz), __fsub_rn(loz, q.z)), 0.0f);
+                        const float dlb = dist2<false>(gx, gy, gz, eps2);
+                        const float qlb = PB ? __fmaf_rn(tlb, sl, eps2) : __fadd_rn(__fmul_rn(tlb, sl), eps2);
+                        if (dlb >= qlb) {
+                            acc = true;
+                        } else {
+                            const float rx = __fsub_rn(q.x, rp.x), ry = __fsub_rn(q.y, rp.y), rz = __fsub_rn(q.z, rp.z);
+                            const float qr = PB ? __fmaf_rn(trep, sl, eps2) : qlb;
+                            if (dist2<false>(rx, ry, rz, eps2) < qr) opn = true;
+                            else inc = true;
+                        }
+                    }
+                    // undecided cells: the vote of every body, one cell after another
+                    unsigned im = __ballot_sync(0xffffffffu, inc);
+                    while (im) {
+                        const int src = __ffs(im) - 1;
+                        im &= im - 1;
+                        const float qx = __shfl_sync(0xffffffffu, q.x, src);
+                        const float qy = __shfl_sync(0xffffffffu, q.y, src);
+                        const float qz = __shfl_sync(0xffffffffu, q.z, src);
+                        const float ss = __shfl_sync(0xffffffffu, sl, src);
+                        bool pass = true;
+#pragma unroll
+                        for (int k = 0; k < BPL; ++k) {
+                            const float dx = __fsub_rn(qx, pb[k].x);
+                            const float dy = __fsub_rn(qy, pb[k].y);
+                            const float dz = __fsub_rn(qz, pb[k].z);
+                            const float dq = PB ? __fmaf_rn(t0[k], ss, eps2) : __fadd_rn(__fmul_rn(t0[k], ss), eps2);
+                            pass = pass && dist2<false>(dx, dy, dz, eps2) >= dq;
+                        }
+                        const bool all = __all_sync(0xffffffffu, pass);
+                        if (lane == src) {
+                            acc = all;
+                            opn = !all;
+                        }
+                    }
+                    const unsigned am = __ballot_sync(0xffffffffu, acc);
+                    const unsigned om = __ballot_sync(0xffffffffu, opn);
+                    tested += __popc(__ballot_sync(0xffffffffu, chk >= 0));
+                    const int on = __popc(om);
+                    if (ctop + on > cap) {               // group-uniform
+                        walked = false;
+                        break;
+                    }
+                    if (acc) lst[lcnt + __popc(am & lt)] = q;
+                    if (opn) cst[ctop + __popc(om & lt)] = make_int2(chk, min(lv + 1, kMaxDepth - 1));
+                    lcnt += __popc(am);
+                    ctop += on;
+                    __syncwarp();          // list and stack written before they are read
+                    if (lcnt >= 32 || (ctop == 0 && lcnt > 0)) {
+                        eval_list<BPL>(lst, lcnt, pb, eps2, ax, ay, az, eb);
+                        accepted += lcnt;
+                        lcnt = 0;
+                        __syncwarp();      // every lane has read the list before it is refilled
+                    }
+                }
+                if (walked) {
+                    ninter = accepted;
+                    visits = tested;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < BPL; ++k) ax[k] = ay[k] = az[k] = eb[k] = 0.f;
+                    __syncwarp();
+                }
+            } else if (fast) {
+                walked = true;
                 int top = 0;
                 int pushed = 0, opened = -1;
                 int open = root;
@@ -255,7 +451,8 @@ __device__ __forceinline__ void force_walk(const StepParams& p) {
                 }
                 if (ok) ninter = pushed - opened;
                 visits = pushed;
-            } else {
+            }
+            if (!walked) {
                 // Deep trees: per-level (cell, next child) walk (calculateforce.cl:112-172).
                 int depth = 0;
                 int node = root;
@@ -371,20 +568,26 @@ template <int W, bool REF, bool PB, bool FEAT>
 __global__ void __launch_bounds__(kForceThreadsMax) force_kernel(StepParams p) {
     force_walk<W, REF, PB, FEAT>(p);
 }
-template <bool PB, bool FEAT>
+template <bool PB, bool FEAT, bool LIST>
 __global__ void __launch_bounds__(kForceThreadsMax, 3) force_kernel64(StepParams p) {
-    force_walk<64, false, PB, FEAT>(p);
+    force_walk<64, false, PB, FEAT, LIST>(p);
 }
 
 template <int W, bool REF, bool PB, bool FEAT>
 static auto force_entry() {
-    if constexpr (W == 64 && !REF) return force_kernel64<PB, FEAT>;
+    if constexpr (W == 64 && !REF) return force_kernel64<PB, FEAT, false>;
     else return force_kernel<W, REF, PB, FEAT>;
 }
 
 // -------------------------------------------------------------------------------------
 template <int W, bool REF, bool PB>
 static void launch_force_pf(const StepParams& p, bool feat, int grid, int threads, cudaStream_t s) {
+    if constexpr (W == 64 && !REF) {
+        if (p.force_list && !feat) {
+            force_kernel64<PB, false, true><<<grid, threads, force_list_smem_bytes(threads, p.stack_cap), s>>>(p);
+            return;
+        }
+    }
     const size_t sm = force_smem_bytes<W>(threads, p.stack_cap);
     if (feat) force_entry<W, REF, PB, true>()<<<grid, threads, sm, s>>>(p);
     else force_entry<W, REF, PB, false>()<<<grid, threads, sm, s>>>(p);
@@ -415,6 +618,12 @@ static cudaError_t prep_force_w() {
 
 int prepare_force_kernels() {
     cudaError_t e = cudaSuccess, t;
+    if ((t = cudaFuncSetAttribute(force_kernel64<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)force_list_smem_bytes(kForceThreadsMax, kStackCapMax))) != cudaSuccess)
+        e = t;
+    if ((t = cudaFuncSetAttribute(force_kernel64<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)force_list_smem_bytes(kForceThreadsMax, kStackCapMax))) != cudaSuccess)
+        e = t;
     if ((t = prep_force_w<128, false>()) != cudaSuccess) e = t;
     if ((t = prep_force_w<64, false>()) != cudaSuccess) e = t;
     if ((t = prep_force_w<32, false>()) != cudaSuccess) e = t;
@@ -543,7 +752,10 @@ void launch_item_order_reset(int nitems, int* order, int* cost, cudaStream_t s) 
     if (nitems > 0) item_order_reset_kernel<<<(nitems + 255) / 256, 256, 0, s>>>(nitems, order, cost);
 }
 
-int occupancy_force(int vote, bool ref, int threads, int cap, int* blocks_per_sm) {
+int occupancy_force(int vote, bool ref, int threads, int cap, bool list, int* blocks_per_sm) {
+    if (vote == 64 && list)
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel64<false, false, true>,
+                                                             threads, force_list_smem_bytes(threads, cap));
     if (vote == 128)
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<128, false, false, false>,
                                                              threads, force_smem_bytes<128>(threads, cap));

@@ -58,7 +58,7 @@ void launch_wait_selftest(const int* flag, unsigned long long limit_ns, DevState
 void launch_fma_peak(float* sink, int iters, int grid, int block, cudaStream_t s);
 
 int occupancy_sort(int* blocks_per_sm);
-int occupancy_force(int vote, bool ref, int threads, int cap, int* blocks_per_sm);
+int occupancy_force(int vote, bool ref, int threads, int cap, bool list, int* blocks_per_sm);
 int prepare_force_kernels();   // raises the dynamic shared-memory limit of the force kernels
 
 }  // namespace nbh

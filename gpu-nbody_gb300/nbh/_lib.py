@@ -45,7 +45,7 @@ class NbhConfig(C.Structure):
         ("vote_width", C.c_int32), ("arith", C.c_int32), ("precise", C.c_int32),
         ("stage_timing", C.c_int32), ("use_graph", C.c_int32), ("force_threads", C.c_int32),
         ("stack_cap", C.c_int32), ("build_phases", C.c_int32), ("build_buckets", C.c_int32),
-        ("top_phase", C.c_int32), ("reserved", C.c_int32 * 3),
+        ("top_phase", C.c_int32), ("force_list", C.c_int32), ("reserved", C.c_int32 * 2),
     ]
 
 

@@ -35,7 +35,7 @@ def _f32(a):
 def make_config(theta=0.5, eps=0.05, dt=0.025, G=1.0, pool_factor=2.0, vote_width=None,
                 arith=L.NBH_ARITH_FMA, precise=False, stage_timing=False, use_graph=True,
                 device=0, theta2=0.0, eps2=0.0, force_threads=0, stack_cap=0, build_phases=0,
-                build_buckets=0, top_phase=0) -> L.NbhConfig:
+                build_buckets=0, top_phase=0, force_list=0) -> L.NbhConfig:
     cfg = L.NbhConfig()
     L.load().nbh_config_default(C.byref(cfg))
     cfg.device = device
@@ -51,6 +51,7 @@ def make_config(theta=0.5, eps=0.05, dt=0.025, G=1.0, pool_factor=2.0, vote_widt
     cfg.force_threads, cfg.stack_cap, cfg.build_phases = force_threads, stack_cap, build_phases
     cfg.build_buckets = build_buckets
     cfg.top_phase = top_phase
+    cfg.force_list = force_list
     return cfg
 
 

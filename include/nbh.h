@@ -88,7 +88,9 @@ typedef struct nbh_config {
                               (0: 128); set by nbh_autotune */
     int32_t stack_cap;     /* entries of each vote group's shared-memory stack, 64..256, a
                               multiple of 8 (0: 256); trees deeper than (cap - 8) / 7 + 1
-                              levels take the per-level walk */
+                              levels take the per-level walk; in the list walk (force_list)
+                              the cells whose children are pending, and a group that would
+                              hold more restarts on the per-level walk */
     int32_t build_phases;  /* octree insertion launches: 1 (one pass), 3 or 5 (0: 5) */
     int32_t build_buckets; /* 1 (or 0, the default): with 5 phases the lock phases insert a
                               1/16 sample of the bodies and every other body joins the
@@ -104,7 +106,15 @@ typedef struct nbh_config {
                               0 (default): one block up to 512 * 256 bodies per universe,
                               eight up to 8192 * 256, the global locks above (the measured
                               fastest); nbh_autotune times all three where possible */
-    int32_t reserved[3];
+    int32_t force_list;    /* the 64-wide walk (fixed or per-body angle, without feature
+                              recording): 1 decides each tested child on its own lane (the
+                              group's bounding box and its most central body settle most
+                              votes) and evaluates the accepted records from a list in shared
+                              memory; 2 visits one child at a time with the vote of every
+                              body.  The same interactions either way; the sums may differ in
+                              the last bits (list order).  0: the default, 1 except in precise
+                              mode, which keeps the reference's order of accumulation */
+    int32_t reserved[2];
 } nbh_config;
 
 /* Fills *cfg with the defaults: theta 0.5, eps 0.05, dt 0.025, G 1, pool 2.0,

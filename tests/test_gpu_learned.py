@@ -122,6 +122,37 @@ def test_per_body_theta_walk_matches_oracle(vote, group):
     np.testing.assert_allclose(eb, o.ebound(), rtol=1e-4, atol=1e-12)
 
 
+@pytest.mark.parametrize("group,force_list", [(0, 1), (1, 1), (0, 2)])
+def test_steps_between_evaluations_walk_with_the_model_angles(group, force_list):
+    """With the model evaluated every 4 steps, the step after a bound-recording step
+    evaluates it and walks with its per-body angles without recording (at width 64 the list
+    walk, whose box test takes the group's smallest angle and whose representative its own).
+    That walk equals the oracle's with the same angles at the same positions: the same
+    interactions, accelerations within the FMA tolerance."""
+    from nbh import learned as LR
+    n = 30000
+    arrs = plummer(n, seed=8)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=64, force_list=force_list)
+    g.load(*arrs)
+    LR.install(g, _model(5), every=4, group=group)
+    g.step(1)                       # records the error bounds
+    pre = g.read()
+    g.step(1)                       # evaluates the model, then walks with its angles
+    th = LR.read_theta(g)
+    assert np.ptp(th) > 0.05                # the angles differ from body to body
+    post = g.read()
+    inter = g.stats()["interactions"]
+    o = oracle_for(n, theta=0.5, eps=0.05, dt=0.01, vote=64, fma=True)
+    o.load(pre["x"], pre["y"], pre["z"], pre["vx"], pre["vy"], pre["vz"], arrs[6])
+    o.set_theta_body(th)
+    o.set_theta_group(group)
+    o.tree()
+    o.force()
+    assert inter == o.interactions
+    rel, _ = acc_rel({"ax": post["ax"], "ay": post["ay"], "az": post["az"]}, o.state())
+    assert rel.max() <= 1e-4 and np.median(rel) <= 2e-6, (rel.max(), np.median(rel))
+
+
 def test_theta_stage_is_timed_on_its_own():
     """With stage timing, the learned-angle stage (features + MLP) gets its own time: zero
     without a model, positive with one, and part of the step's time."""

@@ -296,6 +296,52 @@ def test_vote64_matches_oracle_one_step(vote, n):
         assert np.abs(gs[k] - os_[k]).max() <= 1e-5 * max(1.0, np.abs(os_[k]).max())
 
 
+@pytest.mark.parametrize("force_list,cap,theta", [(1, 256, 0.5), (2, 256, 0.5), (1, 64, 0.5), (1, 256, 0.15),
+                                                 (1, 64, 0.15)],
+                         ids=["list-walk", "per-visit-walk", "list-walk-overflow-restarts", "list-walk-small-angle",
+                              "list-walk-small-angle-overflow"])
+def test_list_walk_matches_oracle(force_list, cap, theta):
+    """The 64-wide walk in both forms: the lane-parallel list walk (box and representative
+    decide most votes, accepted records evaluated from a shared-memory list) and one child at
+    a time.  Both take the oracle's votes: the same interactions and depth-first order,
+    accelerations within the FMA tolerance.  A 64-cell stack overflows for part of the groups
+    (up to ~80 pending cells at theta 0.5, ~140 at 0.15 on this sphere), which restart on the
+    per-level walk, with the same result."""
+    n = 20000
+    arrs = plummer(n, seed=91)
+    g = gpu_sim(theta=theta, eps=0.05, dt=0.01, vote_width=64, force_list=force_list, stack_cap=cap)
+    g.load(*arrs)
+    o = oracle_for(n, theta=theta, eps=0.05, dt=0.01, vote=64, fma=True)
+    o.load(*arrs)
+    g.step(2)
+    o.step(2)
+    gs, os_ = g.read(), o.state()
+    assert g.stats()["interactions"] == o.interactions
+    np.testing.assert_array_equal(g.tree()["sorted"], o.tree_arrays()["sorted"])
+    rel, _ = acc_rel(gs, os_)
+    assert rel.max() <= FMA_ACC_REL_MAX, rel.max()
+    assert np.median(rel) <= FMA_ACC_REL_MEDIAN, np.median(rel)
+
+
+def test_list_walk_and_per_visit_walk_agree_at_1m():
+    """1M-body Plummer sphere: the list walk and the per-visit walk accept the same nodes (the
+    same interaction count) and their sums differ only by rounding order."""
+    n = 1 << 20
+    arrs = plummer(n, seed=2024)
+    acc, inter = {}, {}
+    for fl in (1, 2):
+        g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=64, force_list=fl)
+        g.load(*arrs)
+        g.step(1)
+        r = g.read()
+        acc[fl] = np.stack([r["ax"], r["ay"], r["az"]]).astype(np.float64)
+        inter[fl] = g.stats()["interactions"]
+        g.close()
+    assert inter[1] == inter[2]
+    rel = np.linalg.norm(acc[1] - acc[2], axis=0) / np.linalg.norm(acc[2], axis=0)
+    assert rel.max() <= 1e-4 and np.median(rel) <= 2e-6, (rel.max(), np.median(rel))
+
+
 @pytest.mark.parametrize("vote", [64, 128])
 def test_vote64_batch_of_universes(vote):
     """Vote widths 64 and 128 over uneven universes: items never straddle a universe
