@@ -27,11 +27,14 @@ constexpr size_t force_smem_bytes(int threads, int cap) {
 }
 
 // The list walk (64-wide groups): per group, the records of accepted nodes awaiting
-// evaluation (at most 31 wait after an evaluation and one round adds at most 32) and a
-// stack of `cap` cells whose children are still to be tested, with their levels (a
-// 64-entry stack also holds the per-level walk's 2 * kMaxDepth ints).
+// evaluation (at most 31 wait after an evaluation and one round adds at most 32) with each
+// record's full cell width^2 (for the error bound; 0 for a body), the undecided cells of a
+// round (at most 32), and a stack of `cap` cells whose children are still to be tested,
+// with their levels (a 64-entry stack also holds the per-level walk's 2 * kMaxDepth ints).
 constexpr int kListCap = 64;
-constexpr size_t list_group_bytes(int cap) { return kListCap * sizeof(float4) + (size_t)cap * sizeof(int2); }
+constexpr size_t list_group_bytes(int cap) {
+    return kListCap * (sizeof(float4) + sizeof(float)) + 32 * sizeof(float4) + (size_t)cap * sizeof(int2);
+}
 constexpr size_t force_list_smem_bytes(int threads, int cap) { return (size_t)(threads / 32) * list_group_bytes(cap); }
 static_assert(kStackCapMin * sizeof(int2) >= 2 * kMaxDepth * sizeof(int), "the per-level walk fits the cell stack");
 
@@ -76,21 +79,43 @@ __device__ __forceinline__ float dist2(const float dx, const float dy, const flo
         return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmaf_rn(dz, dz, eps2)));
 }
 
-// Evaluate the first cnt records of a group's list for the lane's bodies, in list order.
-template <int BPL>
-__device__ __forceinline__ void eval_list(const float4* lst, const int cnt, const float4 (&pb)[BPL],
-                                          const float eps2, float (&ax)[BPL], float (&ay)[BPL], float (&az)[BPL],
-                                          float (&eb)[BPL]) {
-#pragma unroll 4
-    for (int i = 0; i < cnt; ++i) {
+// The first 32 records, unrolled by 8.
+template <int BPL, bool FEAT>
+__device__ __forceinline__ void eval_list32(const float4* lst, const float* lw, const float4 (&pb)[BPL],
+                                            const float eps2, float (&ax)[BPL], float (&ay)[BPL], float (&az)[BPL],
+                                            float (&eb)[BPL]) {
+#pragma unroll 8
+    for (int i = 0; i < 32; ++i) {
         const float4 q = lst[i];
+        const float s2 = FEAT ? lw[i] : 0.0f;
 #pragma unroll
         for (int k = 0; k < BPL; ++k) {
             const float dx = __fsub_rn(q.x, pb[k].x);
             const float dy = __fsub_rn(q.y, pb[k].y);
             const float dz = __fsub_rn(q.z, pb[k].z);
             const float d2 = dist2<false>(dx, dy, dz, eps2);
-            interact<false, false>(q, dx, dy, dz, d2, ax[k], ay[k], az[k], eb[k], 0.0f);
+            interact<false, FEAT>(q, dx, dy, dz, d2, ax[k], ay[k], az[k], eb[k], s2);
+        }
+    }
+}
+
+// Evaluate the first cnt records of a group's list for the lane's bodies, in list order
+// (with FEAT also their error bounds, from the widths in lw).
+template <int BPL, bool FEAT>
+__device__ __forceinline__ void eval_list(const float4* lst, const float* lw, const int cnt, const float4 (&pb)[BPL],
+                                          const float eps2, float (&ax)[BPL], float (&ay)[BPL], float (&az)[BPL],
+                                          float (&eb)[BPL]) {
+#pragma unroll 4
+    for (int i = 0; i < cnt; ++i) {
+        const float4 q = lst[i];
+        const float s2 = FEAT ? lw[i] : 0.0f;
+#pragma unroll
+        for (int k = 0; k < BPL; ++k) {
+            const float dx = __fsub_rn(q.x, pb[k].x);
+            const float dy = __fsub_rn(q.y, pb[k].y);
+            const float dz = __fsub_rn(q.z, pb[k].z);
+            const float d2 = dist2<false>(dx, dy, dz, eps2);
+            interact<false, FEAT>(q, dx, dy, dz, d2, ax[k], ay[k], az[k], eb[k], s2);
         }
     }
 }
@@ -126,7 +151,7 @@ __device__ __forceinline__ void eval_list(const float4* lst, const int cnt, cons
 // p.feat_gate set, a launch that does not match the step's place in the learned-theta
 // schedule returns at once (the step graph holds a recording and a plain launch).
 //
-// LIST (W = 64, FMA arithmetic, no features): the same votes, taken lane-parallel.  Each
+// LIST (W = 64, FMA arithmetic): the same votes, taken lane-parallel.  Each
 // round the lanes take the children of up to four cells from the group's cell stack, one
 // child per lane (8 lanes per cell), and decide each child on its own lane: a body is
 // accepted; a cell is accepted when even the group's bounding box passes the test (the
@@ -134,14 +159,14 @@ __device__ __forceinline__ void eval_list(const float4* lst, const int cnt, cons
 // the fused squares and the comparison are monotone, so every body's own test passes), and
 // opened when the group's body nearest the box centre fails it (then the vote fails).  Only
 // the remaining cells take the vote of every body, one after another.  Accepted records go
-// to a list in shared memory, evaluated 32 to 63 at a time in a loop of arithmetic alone:
+// to a list in shared memory, evaluated 32 at a time in a loop of arithmetic alone:
 // the same interactions as the per-visit walk, accumulated in list order (rounding may
 // differ from it in the last bits).  A cell stack that would overflow restarts the group
 // on the per-level walk (stack_cap entries: 256 by default, enough for every 64-body group
 // of the benchmarked spheres, which needed at most 99).
 template <int W, bool REF, bool PB, bool FEAT, bool LIST = false>
 __device__ __forceinline__ void force_walk(const StepParams& p) {
-    static_assert(!LIST || (W == 64 && !REF && !FEAT), "the list walk is the 64-wide FMA walk without features");
+    static_assert(!LIST || (W == 64 && !REF), "the list walk is the 64-wide FMA walk");
     if (load_status(p.st)) return;
     if (p.feat_gate && theta_bound_step(p.st, p.st->step) != (p.feat_gate == 1)) return;
     constexpr int GL = group_lanes<W>();            // lanes per group
@@ -162,7 +187,9 @@ __device__ __forceinline__ void force_walk(const StepParams& p) {
     int2* const se = se_all + grp * cap;             // (node index, bits of threshold or level factor)
     // list walk: the group's list of accepted records and its stack of (cell, level)
     float4* const lst = reinterpret_cast<float4*>(smem_raw + (size_t)grp * list_group_bytes(cap));
-    int2* const cst = reinterpret_cast<int2*>(lst + kListCap);
+    float* const lw = reinterpret_cast<float*>(lst + kListCap);
+    float4* const ud = reinterpret_cast<float4*>(lw + kListCap);   // undecided cells of a round
+    int2* const cst = reinterpret_cast<int2*>(ud + 32);
     // deep-tree walk: (cell, next) per level
     int* const snode = LIST ? reinterpret_cast<int*>(cst) : reinterpret_cast<int*>(se);
     int* const snext = snode + kMaxDepth;
@@ -325,27 +352,31 @@ __device__ __forceinline__ void force_walk(const StepParams& p) {
                         }
                     }
                     // undecided cells: the vote of every body, one cell after another
-                    unsigned im = __ballot_sync(0xffffffffu, inc);
-                    while (im) {
-                        const int src = __ffs(im) - 1;
-                        im &= im - 1;
-                        const float qx = __shfl_sync(0xffffffffu, q.x, src);
-                        const float qy = __shfl_sync(0xffffffffu, q.y, src);
-                        const float qz = __shfl_sync(0xffffffffu, q.z, src);
-                        const float ss = __shfl_sync(0xffffffffu, sl, src);
-                        bool pass = true;
+                    const unsigned im = __ballot_sync(0xffffffffu, inc);
+                    if (im) {
+                        // their records go to shared memory and every lane reads them back in turn
+                        const int nud = __popc(im);
+                        const int mine = __popc(im & lt);
+                        if (inc) ud[mine] = make_float4(q.x, q.y, q.z, sl);
+                        __syncwarp();
+                        unsigned res = 0;
+                        for (int j = 0; j < nud; ++j) {
+                            const float4 uq = ud[j];
+                            bool pass = true;
 #pragma unroll
-                        for (int k = 0; k < BPL; ++k) {
-                            const float dx = __fsub_rn(qx, pb[k].x);
-                            const float dy = __fsub_rn(qy, pb[k].y);
-                            const float dz = __fsub_rn(qz, pb[k].z);
-                            const float dq = PB ? __fmaf_rn(t0[k], ss, eps2) : __fadd_rn(__fmul_rn(t0[k], ss), eps2);
-                            pass = pass && dist2<false>(dx, dy, dz, eps2) >= dq;
+                            for (int k = 0; k < BPL; ++k) {
+                                const float dx = __fsub_rn(uq.x, pb[k].x);
+                                const float dy = __fsub_rn(uq.y, pb[k].y);
+                                const float dz = __fsub_rn(uq.z, pb[k].z);
+                                const float dq =
+                                    PB ? __fmaf_rn(t0[k], uq.w, eps2) : __fadd_rn(__fmul_rn(t0[k], uq.w), eps2);
+                                pass = pass && dist2<false>(dx, dy, dz, eps2) >= dq;
+                            }
+                            res |= (__all_sync(0xffffffffu, pass) ? 1u : 0u) << j;
                         }
-                        const bool all = __all_sync(0xffffffffu, pass);
-                        if (lane == src) {
-                            acc = all;
-                            opn = !all;
+                        if (inc) {
+                            acc = (res >> mine) & 1u;
+                            opn = !acc;
                         }
                     }
                     const unsigned am = __ballot_sync(0xffffffffu, acc);
@@ -356,16 +387,34 @@ __device__ __forceinline__ void force_walk(const StepParams& p) {
                         walked = false;
                         break;
                     }
-                    if (acc) lst[lcnt + __popc(am & lt)] = q;
+                    if (acc) {
+                        const int at = lcnt + __popc(am & lt);
+                        lst[at] = q;
+                        // full width^2 of an accepted cell, r^2 * 4^-level (0 for a body)
+                        if constexpr (FEAT) lw[at] = chk >= nbody ? __fmul_rn(rr, sl) : 0.0f;
+                    }
                     if (opn) cst[ctop + __popc(om & lt)] = make_int2(chk, min(lv + 1, kMaxDepth - 1));
                     lcnt += __popc(am);
                     ctop += on;
                     __syncwarp();          // list and stack written before they are read
-                    if (lcnt >= 32 || (ctop == 0 && lcnt > 0)) {
-                        eval_list<BPL>(lst, lcnt, pb, eps2, ax, ay, az, eb);
+                    if (lcnt >= 32) {
+                        // 32 records at a time; the rest (at most 31) move to the front
+                        eval_list32<BPL, FEAT>(lst, lw, pb, eps2, ax, ay, az, eb);
+                        accepted += 32;
+                        __syncwarp();
+                        const int rest = lcnt - 32;
+                        if (lane < rest) {
+                            lst[lane] = lst[32 + lane];
+                            if constexpr (FEAT) lw[lane] = lw[32 + lane];
+                        }
+                        lcnt = rest;
+                        __syncwarp();
+                    }
+                    if (ctop == 0 && lcnt > 0) {
+                        eval_list<BPL, FEAT>(lst, lw, lcnt, pb, eps2, ax, ay, az, eb);
                         accepted += lcnt;
                         lcnt = 0;
-                        __syncwarp();      // every lane has read the list before it is refilled
+                        __syncwarp();
                     }
                 }
                 if (walked) {
@@ -583,8 +632,10 @@ static auto force_entry() {
 template <int W, bool REF, bool PB>
 static void launch_force_pf(const StepParams& p, bool feat, int grid, int threads, cudaStream_t s) {
     if constexpr (W == 64 && !REF) {
-        if (p.force_list && !feat) {
-            force_kernel64<PB, false, true><<<grid, threads, force_list_smem_bytes(threads, p.stack_cap), s>>>(p);
+        if (p.force_list) {
+            const size_t sm = force_list_smem_bytes(threads, p.stack_cap);
+            if (feat) force_kernel64<PB, true, true><<<grid, threads, sm, s>>>(p);
+            else force_kernel64<PB, false, true><<<grid, threads, sm, s>>>(p);
             return;
         }
     }
@@ -622,6 +673,12 @@ int prepare_force_kernels() {
                                   (int)force_list_smem_bytes(kForceThreadsMax, kStackCapMax))) != cudaSuccess)
         e = t;
     if ((t = cudaFuncSetAttribute(force_kernel64<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)force_list_smem_bytes(kForceThreadsMax, kStackCapMax))) != cudaSuccess)
+        e = t;
+    if ((t = cudaFuncSetAttribute(force_kernel64<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)force_list_smem_bytes(kForceThreadsMax, kStackCapMax))) != cudaSuccess)
+        e = t;
+    if ((t = cudaFuncSetAttribute(force_kernel64<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)force_list_smem_bytes(kForceThreadsMax, kStackCapMax))) != cudaSuccess)
         e = t;
     if ((t = prep_force_w<128, false>()) != cudaSuccess) e = t;
