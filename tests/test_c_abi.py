@@ -38,7 +38,7 @@ def test_config_struct_layout_matches_header():
     assert (cfg.theta, cfg.G, cfg.pool_factor) == (0.5, 1.0, 2.0)
     assert cfg.eps == pytest.approx(0.05) and cfg.dt == pytest.approx(0.025)
     assert cfg.vote_width == 64 and cfg.arith == L.NBH_ARITH_FMA and cfg.use_graph == 1
-    assert C.sizeof(L.NbhConfig) == 4 * (2 + 7 + 10 + 3)
+    assert C.sizeof(L.NbhConfig) == 4 * (2 + 7 + 11 + 2)
 
 
 def test_struct_layouts_match_the_c_compiler(tmp_path):
@@ -66,6 +66,21 @@ def test_struct_layouts_match_the_c_compiler(tmp_path):
         assert int(out[cname]) == C.sizeof(py), cname
         for fname, _ in py._fields_:
             assert int(out["%s.%s" % (cname, fname)]) == getattr(py, fname).offset, (cname, fname)
+
+
+def test_java_binding_text_matches_the_structs():
+    """The Java FFM binding in INTEGRATION.md lays nbh_config out field by field and allocates
+    nbh_tune by size: the field names, their order, the reserved tail and the size equal the
+    header's (a stale size would let nbh_autotune write past the Java allocation)."""
+    txt = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    block = txt[txt.index("StructLayout CONFIG"):]
+    block = block[:block.index(";")]
+    names = re.findall(r'JAVA_(?:INT|FLOAT)\.withName\("(\w+)"\)', block)
+    fields = [f for f, _ in L.NbhConfig._fields_]
+    assert names == fields[:-1] and fields[-1] == "reserved"
+    nres = int(re.search(r"sequenceLayout\((\d+), JAVA_INT\)\.withName\(\"reserved\"\)", block).group(1))
+    assert nres == getattr(L.NbhConfig, "reserved").size // 4
+    assert [int(v) for v in re.findall(r"arena\.allocate\((\d+), 4\)", txt)] == [C.sizeof(L.NbhTune)]
 
 
 def test_mlp_constants_match_header_and_network_shape():
