@@ -50,7 +50,7 @@ struct nbh_sim {
     int theta_group = 0;           // 1: each vote group walks with its smallest angle
     int force_threads = 128;       // force launch geometry (nbh_autotune)
     int stack_cap = 256;
-    bool force_list = true;        // 64-wide walks without features: the lane-parallel list walk
+    bool force_list = true;        // whole-warp FMA walks (vote width 32, 64, 128): the lane-parallel list walk
     int build_phases = 5;          // octree insertion launches
     bool build_buckets = true;     // lock phases insert a sample, the rest is built per slot
     int top_phase = 0;             // config: where the first phase may build in shared memory
@@ -1291,7 +1291,7 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
         // the list walk's stack holds cells, and 256 of them are never slower: only block
         // sizes are timed (and the geometry in place)
         const bool in_place = g.first == sim->force_threads && g.second == sim->stack_cap;
-        if (vote == 64 && sim->force_list && g.second != 256 && !in_place) continue;
+        if (vote >= 32 && !ref && sim->force_list && g.second != 256 && !in_place) continue;
         int occ = 0;
         if ((err = static_cast<cudaError_t>(occupancy_force(vote, ref, g.first, g.second, sim->force_list, &occ))) !=
             cudaSuccess)

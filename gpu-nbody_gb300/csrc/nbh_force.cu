@@ -151,7 +151,8 @@ __device__ __forceinline__ void eval_list(const float4* lst, const float* lw, co
 // p.feat_gate set, a launch that does not match the step's place in the learned-theta
 // schedule returns at once (the step graph holds a recording and a plain launch).
 //
-// LIST (W = 64, FMA arithmetic): the same votes, taken lane-parallel.  Each
+// LIST (W = 32, 64 or 128: one warp per group; FMA arithmetic): the same votes, taken
+// lane-parallel.  Each
 // round the lanes take the children of up to four cells from the group's cell stack, one
 // child per lane (8 lanes per cell), and decide each child on its own lane: a body is
 // accepted; a cell is accepted when even the group's bounding box passes the test (the
@@ -166,7 +167,7 @@ __device__ __forceinline__ void eval_list(const float4* lst, const float* lw, co
 // of the benchmarked spheres, which needed at most 99).
 template <int W, bool REF, bool PB, bool FEAT, bool LIST = false>
 __device__ __forceinline__ void force_walk(const StepParams& p) {
-    static_assert(!LIST || (W == 64 && !REF), "the list walk is the 64-wide FMA walk");
+    static_assert(!LIST || (W >= 32 && !REF), "the list walk takes whole-warp groups and FMA arithmetic");
     if (load_status(p.st)) return;
     if (p.feat_gate && theta_bound_step(p.st, p.st->step) != (p.feat_gate == 1)) return;
     constexpr int GL = group_lanes<W>();            // lanes per group
@@ -259,8 +260,12 @@ __device__ __forceinline__ void force_walk(const StepParams& p) {
             if constexpr (LIST) {
                 walked = true;
                 // the group's bounding box (lanes past the end hold the first body)
-                float lox = fminf(pb[0].x, pb[1].x), loy = fminf(pb[0].y, pb[1].y), loz = fminf(pb[0].z, pb[1].z);
-                float hix = fmaxf(pb[0].x, pb[1].x), hiy = fmaxf(pb[0].y, pb[1].y), hiz = fmaxf(pb[0].z, pb[1].z);
+                float lox = pb[0].x, loy = pb[0].y, loz = pb[0].z, hix = pb[0].x, hiy = pb[0].y, hiz = pb[0].z;
+#pragma unroll
+                for (int k = 1; k < BPL; ++k) {
+                    lox = fminf(lox, pb[k].x), loy = fminf(loy, pb[k].y), loz = fminf(loz, pb[k].z);
+                    hix = fmaxf(hix, pb[k].x), hiy = fmaxf(hiy, pb[k].y), hiz = fmaxf(hiz, pb[k].z);
+                }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
                     lox = fminf(lox, __shfl_xor_sync(0xffffffffu, lox, o));
@@ -613,29 +618,29 @@ __device__ __forceinline__ void force_walk(const StepParams& p) {
 // with less overlap in the visit loop: 1.6 % slower, the fixed-angle walk 0.7 % slower).
 // The other widths keep the compiler's own choice (with the same hint the 32-wide walk ran
 // 5-10 % slower).
-template <int W, bool REF, bool PB, bool FEAT>
+template <int W, bool REF, bool PB, bool FEAT, bool LIST = false>
 __global__ void __launch_bounds__(kForceThreadsMax) force_kernel(StepParams p) {
-    force_walk<W, REF, PB, FEAT>(p);
+    force_walk<W, REF, PB, FEAT, LIST>(p);
 }
 template <bool PB, bool FEAT, bool LIST>
 __global__ void __launch_bounds__(kForceThreadsMax, 3) force_kernel64(StepParams p) {
     force_walk<64, false, PB, FEAT, LIST>(p);
 }
 
-template <int W, bool REF, bool PB, bool FEAT>
+template <int W, bool REF, bool PB, bool FEAT, bool LIST = false>
 static auto force_entry() {
-    if constexpr (W == 64 && !REF) return force_kernel64<PB, FEAT, false>;
-    else return force_kernel<W, REF, PB, FEAT>;
+    if constexpr (W == 64 && !REF) return force_kernel64<PB, FEAT, LIST>;
+    else return force_kernel<W, REF, PB, FEAT, LIST>;
 }
 
 // -------------------------------------------------------------------------------------
 template <int W, bool REF, bool PB>
 static void launch_force_pf(const StepParams& p, bool feat, int grid, int threads, cudaStream_t s) {
-    if constexpr (W == 64 && !REF) {
+    if constexpr (W >= 32 && !REF) {
         if (p.force_list) {
             const size_t sm = force_list_smem_bytes(threads, p.stack_cap);
-            if (feat) force_kernel64<PB, true, true><<<grid, threads, sm, s>>>(p);
-            else force_kernel64<PB, false, true><<<grid, threads, sm, s>>>(p);
+            if (feat) force_entry<W, false, PB, true, true>()<<<grid, threads, sm, s>>>(p);
+            else force_entry<W, false, PB, false, true>()<<<grid, threads, sm, s>>>(p);
             return;
         }
     }
@@ -667,20 +672,30 @@ static cudaError_t prep_force_w() {
     return e;
 }
 
+template <int W>
+static cudaError_t prep_list_w() {
+    cudaError_t e = cudaSuccess, t;
+    const int sm = (int)force_list_smem_bytes(kForceThreadsMax, kStackCapMax);
+    if ((t = cudaFuncSetAttribute(force_entry<W, false, false, false, true>(),
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, sm)) != cudaSuccess)
+        e = t;
+    if ((t = cudaFuncSetAttribute(force_entry<W, false, false, true, true>(),
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, sm)) != cudaSuccess)
+        e = t;
+    if ((t = cudaFuncSetAttribute(force_entry<W, false, true, false, true>(),
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, sm)) != cudaSuccess)
+        e = t;
+    if ((t = cudaFuncSetAttribute(force_entry<W, false, true, true, true>(),
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, sm)) != cudaSuccess)
+        e = t;
+    return e;
+}
+
 int prepare_force_kernels() {
     cudaError_t e = cudaSuccess, t;
-    if ((t = cudaFuncSetAttribute(force_kernel64<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)force_list_smem_bytes(kForceThreadsMax, kStackCapMax))) != cudaSuccess)
-        e = t;
-    if ((t = cudaFuncSetAttribute(force_kernel64<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)force_list_smem_bytes(kForceThreadsMax, kStackCapMax))) != cudaSuccess)
-        e = t;
-    if ((t = cudaFuncSetAttribute(force_kernel64<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)force_list_smem_bytes(kForceThreadsMax, kStackCapMax))) != cudaSuccess)
-        e = t;
-    if ((t = cudaFuncSetAttribute(force_kernel64<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)force_list_smem_bytes(kForceThreadsMax, kStackCapMax))) != cudaSuccess)
-        e = t;
+    if ((t = prep_list_w<32>()) != cudaSuccess) e = t;
+    if ((t = prep_list_w<64>()) != cudaSuccess) e = t;
+    if ((t = prep_list_w<128>()) != cudaSuccess) e = t;
     if ((t = prep_force_w<128, false>()) != cudaSuccess) e = t;
     if ((t = prep_force_w<64, false>()) != cudaSuccess) e = t;
     if ((t = prep_force_w<32, false>()) != cudaSuccess) e = t;
@@ -810,9 +825,17 @@ void launch_item_order_reset(int nitems, int* order, int* cost, cudaStream_t s) 
 }
 
 int occupancy_force(int vote, bool ref, int threads, int cap, bool list, int* blocks_per_sm) {
-    if (vote == 64 && list)
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel64<false, false, true>,
-                                                             threads, force_list_smem_bytes(threads, cap));
+    if (list && !ref && vote >= 32) {
+        const size_t sm = force_list_smem_bytes(threads, cap);
+        if (vote == 128)
+            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_entry<128, false, false, false, true>(),
+                                                                 threads, sm);
+        if (vote == 64)
+            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_entry<64, false, false, false, true>(),
+                                                                 threads, sm);
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_entry<32, false, false, false, true>(),
+                                                             threads, sm);
+    }
     if (vote == 128)
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, force_kernel<128, false, false, false>,
                                                              threads, force_smem_bytes<128>(threads, cap));

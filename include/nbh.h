@@ -106,14 +106,15 @@ typedef struct nbh_config {
                               0 (default): one block up to 512 * 256 bodies per universe,
                               eight up to 8192 * 256, the global locks above (the measured
                               fastest); nbh_autotune times all three where possible */
-    int32_t force_list;    /* the 64-wide walk (fixed or per-body angle, without feature
-                              recording): 1 decides each tested child on its own lane (the
-                              group's bounding box and its most central body settle most
-                              votes) and evaluates the accepted records from a list in shared
-                              memory; 2 visits one child at a time with the vote of every
-                              body.  The same interactions either way; the sums may differ in
-                              the last bits (list order).  0: the default, 1 except in precise
-                              mode, which keeps the reference's order of accumulation */
+    int32_t force_list;    /* the whole-warp walks (vote width 32, 64 or 128; FMA arithmetic;
+                              fixed or per-body angle): 1 decides each tested child on its own
+                              lane (the group's bounding box and its most central body settle
+                              most votes) and evaluates the accepted records from a list in
+                              shared memory; 2 visits one child at a time with the vote of
+                              every body.  The same interactions either way; the sums may
+                              differ in the last bits (list order).  0: the default, 1 except
+                              in precise mode, which keeps the reference's order of
+                              accumulation */
     int32_t reserved[2];
 } nbh_config;
 

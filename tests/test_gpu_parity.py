@@ -296,22 +296,26 @@ def test_vote64_matches_oracle_one_step(vote, n):
         assert np.abs(gs[k] - os_[k]).max() <= 1e-5 * max(1.0, np.abs(os_[k]).max())
 
 
-@pytest.mark.parametrize("force_list,cap,theta", [(1, 256, 0.5), (2, 256, 0.5), (1, 64, 0.5), (1, 256, 0.15),
-                                                 (1, 64, 0.15)],
+@pytest.mark.parametrize("vote,force_list,cap,theta",
+                         [(64, 1, 256, 0.5), (64, 2, 256, 0.5), (64, 1, 64, 0.5), (64, 1, 256, 0.15),
+                          (64, 1, 64, 0.15), (32, 1, 256, 0.5), (32, 2, 256, 0.5), (32, 1, 64, 0.15),
+                          (128, 1, 256, 0.5), (128, 1, 64, 0.15)],
                          ids=["list-walk", "per-visit-walk", "list-walk-overflow-restarts", "list-walk-small-angle",
-                              "list-walk-small-angle-overflow"])
-def test_list_walk_matches_oracle(force_list, cap, theta):
-    """The 64-wide walk in both forms: the lane-parallel list walk (box and representative
-    decide most votes, accepted records evaluated from a shared-memory list) and one child at
-    a time.  Both take the oracle's votes: the same interactions and depth-first order,
-    accelerations within the FMA tolerance.  A 64-cell stack overflows for part of the groups
-    (up to ~80 pending cells at theta 0.5, ~140 at 0.15 on this sphere), which restart on the
-    per-level walk, with the same result."""
+                              "list-walk-small-angle-overflow", "list-walk-32", "per-visit-walk-32",
+                              "list-walk-32-small-angle-overflow", "list-walk-128", "list-walk-128-small-angle-overflow"])
+def test_list_walk_matches_oracle(vote, force_list, cap, theta):
+    """The whole-warp walks (vote widths 32, 64, 128) in both forms: the lane-parallel list
+    walk (box and representative decide most votes, accepted records evaluated from a
+    shared-memory list) and one child at a time.  Both take the oracle's votes: the same
+    interactions and depth-first order, accelerations within the FMA tolerance.  A 64-cell
+    stack overflows for part of the groups (up to ~80 pending cells at theta 0.5, ~140 at
+    0.15 on this sphere at width 64), which restart on the per-level walk, with the same
+    result."""
     n = 20000
     arrs = plummer(n, seed=91)
-    g = gpu_sim(theta=theta, eps=0.05, dt=0.01, vote_width=64, force_list=force_list, stack_cap=cap)
+    g = gpu_sim(theta=theta, eps=0.05, dt=0.01, vote_width=vote, force_list=force_list, stack_cap=cap)
     g.load(*arrs)
-    o = oracle_for(n, theta=theta, eps=0.05, dt=0.01, vote=64, fma=True)
+    o = oracle_for(n, theta=theta, eps=0.05, dt=0.01, vote=vote, fma=True)
     o.load(*arrs)
     g.step(2)
     o.step(2)
