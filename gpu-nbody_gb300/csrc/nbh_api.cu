@@ -1722,9 +1722,16 @@ int nbh_mlp_train(int32_t device, float* params, const float* X, const float* T,
     int e;
     if ((e = train_setup(b, params, X, T, n))) return e;
     cudaStream_t s = nullptr;
+    // The rate falls linearly to zero over the last 30 % of the steps.  The pinball loss's
+    // gradient does not shrink near its minimum, so at a constant rate the fitted quantile
+    // keeps oscillating: in an FP64 replay of these steps (q = 0.2, 20,000 samples) the share
+    // of targets below the fit moved between 0.11 and 0.30 from one hundred steps to the
+    // next; with the decay it ends at 0.198-0.202.
+    const int t_decay = iters - (3 * iters) / 10;
     for (int it = 1; it <= iters; ++it) {
         mlp_grad(b.prm, b.X, b.T, n, quantile, b.w, b.grad, b.loss, s);
-        adam_step(b.prm, b.grad, b.m1, b.m2, lr, it, s);
+        const float lr_t = it <= t_decay ? lr : lr * (float)(iters - it + 1) / (float)(iters - t_decay + 1);
+        adam_step(b.prm, b.grad, b.m1, b.m2, lr_t, it, s);
     }
     // loss of the final parameters
     mlp_grad(b.prm, b.X, b.T, n, quantile, b.w, b.grad, b.loss, s);

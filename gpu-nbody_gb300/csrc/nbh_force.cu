@@ -320,7 +320,7 @@ __device__ __forceinline__ void force_walk(const StepParams& p) {
                 }
                 const unsigned lt = (1u << lane) - 1u;
                 if (lane == 0) cst[0] = make_int2(root, 0);
-                int ctop = 1, lcnt = 0, tested = 0;
+                int ctop = 1, lcnt = 0, opened = 0;    // every tested child is accepted or opened
                 long long accepted = 0;
                 __syncwarp();
                 while (ctop > 0) {
@@ -386,8 +386,8 @@ __device__ __forceinline__ void force_walk(const StepParams& p) {
                     }
                     const unsigned am = __ballot_sync(0xffffffffu, acc);
                     const unsigned om = __ballot_sync(0xffffffffu, opn);
-                    tested += __popc(__ballot_sync(0xffffffffu, chk >= 0));
                     const int on = __popc(om);
+                    opened += on;
                     if (ctop + on > cap) {               // group-uniform
                         walked = false;
                         break;
@@ -424,7 +424,7 @@ __device__ __forceinline__ void force_walk(const StepParams& p) {
                 }
                 if (walked) {
                     ninter = accepted;
-                    visits = tested;
+                    visits = (int)accepted + opened;
                 } else {
 #pragma unroll
                     for (int k = 0; k < BPL; ++k) ax[k] = ay[k] = az[k] = eb[k] = 0.f;

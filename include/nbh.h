@@ -360,7 +360,8 @@ int nbh_theta_features(nbh_sim* sim, float* feat, int32_t use_probe);
 /* Training of the model on the device with FP32 forward/backward kernels: samples X[n*12]
  * (normalised features, row-major), targets T[n] (log theta), pinball loss at `quantile`
  * (the fraction of samples whose target the prediction may exceed).  nbh_mlp_train runs
- * `iters` full-batch Adam steps from params (updated in place) and reports the final loss;
+ * `iters` full-batch Adam steps from params (updated in place), the rate `lr` falling
+ * linearly to zero over the last 30 % of them, and reports the final loss;
  * nbh_mlp_grad returns the gradient and loss of one pass; nbh_mlp_forward the outputs. */
 int nbh_mlp_train(int32_t device, float* params, const float* X, const float* T, int32_t n,
                   float quantile, int32_t iters, float lr, float* loss);

@@ -49,7 +49,9 @@ def test_mlp_training_fits_quantile():
     import mlp_ref
     pred = mlp_ref.forward(m["params"], (X - m["mean"]) * m["inv_std"])
     frac_below = (Y < pred).mean()
-    assert 0.1 <= frac_below <= 0.3, frac_below           # ~20% of targets below the prediction
+    # ~20 % of targets below the prediction: the rate's final decay settles the fitted quantile
+    # (an FP64 replay of the same steps ends at 0.198-0.202 for four data seeds)
+    assert 0.15 <= frac_below <= 0.25, frac_below
     assert np.corrcoef(pred, Y)[0, 1] > 0.9
 
 
