@@ -1223,7 +1223,7 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
     // the lowest median wins (geometries and schedules differ by a few per cent, about the
     // spread of a 3-launch mean from run to run).  Returns the index into `launches`.
     auto refine = [&](const std::vector<std::function<void()>>& launches, int rounds, float* best_median,
-                      cudaError_t* err_out) -> int {
+                      cudaError_t* err_out, std::vector<float>* medians) -> int {
         const size_t k = launches.size();
         std::vector<std::vector<float>> t(k);
         for (int r = 0; r < rounds && *err_out == cudaSuccess; ++r)
@@ -1235,10 +1235,12 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
             }
         int best = 0;
         float bm = 1e30f;
+        medians->assign(k, 1e30f);
         for (size_t i = 0; i < k; ++i) {
             if (t[i].empty()) continue;
             std::sort(t[i].begin(), t[i].end());
             const float m = t[i][t[i].size() / 2];
+            (*medians)[i] = m;
             if (m < bm) {
                 bm = m;
                 best = (int)i;
@@ -1280,6 +1282,7 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
     struct ForceCand {
         float ms;
         int threads, cap, vote, grid;
+        bool in_place;   // the geometry in place before
     };
     std::vector<ForceCand> fcands;
     std::vector<int> votes{vote_before};
@@ -1310,9 +1313,9 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
         err = timed([&] { launch_force(q, vote, ref, false, grid, g.first, s); }, &ms);
         if (err != cudaSuccess) break;
         add_trial(0, g.first, g.second, vote, ms);
-        fcands.push_back({ms, g.first, g.second, vote, grid});
-        if (vote == vote_before && g.first == sim->force_threads && g.second == sim->stack_cap)
-            out->ms_force_before = ms;
+        const bool before = vote == vote_before && g.first == sim->force_threads && g.second == sim->stack_cap;
+        fcands.push_back({ms, g.first, g.second, vote, grid, before});
+        if (before) out->ms_force_before = ms;
         if (ms < best_ms) {
             best_ms = ms;
             best_t = g.first;
@@ -1321,9 +1324,17 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
         }
     }
     if (err == cudaSuccess && fcands.size() > 1) {
-        // the three fastest, timed again alternately; the lowest median is kept
+        // the three fastest and the geometry in place, timed again alternately; the lowest
+        // median is kept, and the one in place is reported from the same runs
         std::sort(fcands.begin(), fcands.end(), [](const ForceCand& x, const ForceCand& y) { return x.ms < y.ms; });
-        fcands.resize(std::min<size_t>(3, fcands.size()));
+        size_t keep = std::min<size_t>(3, fcands.size());
+        for (size_t i = keep; i < fcands.size(); ++i)
+            if (fcands[i].in_place) {
+                std::swap(fcands[keep], fcands[i]);
+                ++keep;
+                break;
+            }
+        fcands.resize(keep);
         std::vector<std::function<void()>> launches;
         for (const auto& c : fcands) {
             StepParams q = step_params(sim);
@@ -1335,8 +1346,11 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
             launches.push_back([=, &s] { launch_force(q, c.vote, ref, false, c.grid, c.threads, s); });
         }
         float med = 0.0f;
-        const int k = refine(launches, 7, &med, &err);
+        std::vector<float> meds;
+        const int k = refine(launches, 7, &med, &err, &meds);
         if (err == cudaSuccess) {
+            for (size_t i = 0; i < fcands.size(); ++i)
+                if (fcands[i].in_place) out->ms_force_before = meds[i];
             best_ms = med;
             best_t = fcands[k].threads;
             best_c = fcands[k].cap;
@@ -1359,6 +1373,7 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
         int phases;
         bool buckets;
         int top;
+        bool in_place;   // the schedule in place before
     };
     std::vector<TreeCand> tcands;
     const int tree_c[13][3] = {{1, 0, 0}, {3, 0, 0}, {5, 0, 0}, {3, 1, 0}, {5, 1, 0},
@@ -1376,10 +1391,10 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
         err = timed([&] { enqueue_tree(sim, p); }, &ms);
         if (err != cudaSuccess) break;
         add_trial(1, tc[0], tc[1], tc[2], ms);
-        tcands.push_back({ms, tc[0], tc[1] != 0, tc[2]});
-        if (tc[0] == phases_before && (tc[1] != 0) == (buckets_before && phases_before != 1) &&
-            tc[2] == (phases_before != 1 ? top_before : 0))
-            out->ms_tree_before = ms;
+        const bool before = tc[0] == phases_before && (tc[1] != 0) == (buckets_before && phases_before != 1) &&
+                            tc[2] == (phases_before != 1 ? top_before : 0);
+        tcands.push_back({ms, tc[0], tc[1] != 0, tc[2], before});
+        if (before) out->ms_tree_before = ms;
         if (ms < best_tree) {
             best_tree = ms;
             best_ph = tc[0];
@@ -1388,9 +1403,16 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
         }
     }
     if (err == cudaSuccess && tcands.size() > 1) {
-        // the two fastest schedules, timed again alternately
+        // the two fastest schedules and the one in place, timed again alternately
         std::sort(tcands.begin(), tcands.end(), [](const TreeCand& x, const TreeCand& y) { return x.ms < y.ms; });
-        tcands.resize(2);
+        size_t keep = 2;
+        for (size_t i = keep; i < tcands.size(); ++i)
+            if (tcands[i].in_place) {
+                std::swap(tcands[keep], tcands[i]);
+                ++keep;
+                break;
+            }
+        tcands.resize(keep);
         std::vector<std::function<void()>> launches;
         for (const auto& c : tcands)
             launches.push_back([=] {
@@ -1402,8 +1424,11 @@ int nbh_autotune(nbh_sim* sim, int32_t flags, nbh_tune* out) {
                 enqueue_tree(sim, p);
             });
         float med = 0.0f;
-        const int k = refine(launches, 7, &med, &err);
+        std::vector<float> meds;
+        const int k = refine(launches, 7, &med, &err, &meds);
         if (err == cudaSuccess) {
+            for (size_t i = 0; i < tcands.size(); ++i)
+                if (tcands[i].in_place) out->ms_tree_before = meds[i];
             best_tree = med;
             best_ph = tcands[k].phases;
             best_bk = tcands[k].buckets;

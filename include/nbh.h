@@ -293,9 +293,10 @@ typedef struct nbh_tune {
     int32_t vote_width;            /* chosen (the sim's own unless NBH_TUNE_VOTE) */
     int32_t max_depth;             /* tree depth the stack capacities were fitted to */
     float   ms_force;              /* force launch of the choice */
-    float   ms_force_before;       /* force launch of the geometry in place before */
+    float   ms_force_before;       /* force launch of the geometry in place before (median
+                                      of the same alternating runs as ms_force) */
     float   ms_tree;               /* tree stages of the choice */
-    float   ms_tree_before;        /* tree stages of the phases in place before */
+    float   ms_tree_before;        /* tree stages of the phases in place before (likewise) */
     int32_t trials;                /* entries used below */
     int32_t trial_kind[NBH_TUNE_MAX_TRIALS];    /* 0 force, 1 tree */
     int32_t trial_a[NBH_TUNE_MAX_TRIALS];       /* threads, or insertion phases */
