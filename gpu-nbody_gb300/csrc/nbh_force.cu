@@ -152,19 +152,18 @@ __device__ __forceinline__ void eval_list(const float4* lst, const float* lw, co
 // schedule returns at once (the step graph holds a recording and a plain launch).
 //
 // LIST (W = 32, 64 or 128: one warp per group; FMA arithmetic): the same votes, taken
-// lane-parallel.  Each
-// round the lanes take the children of up to four cells from the group's cell stack, one
-// child per lane (8 lanes per cell), and decide each child on its own lane: a body is
-// accepted; a cell is accepted when even the group's bounding box passes the test (the
-// box's distance components bound every body's from below, and the rounded subtractions,
-// the fused squares and the comparison are monotone, so every body's own test passes), and
-// opened when the group's body nearest the box centre fails it (then the vote fails).  Only
-// the remaining cells take the vote of every body, one after another.  Accepted records go
-// to a list in shared memory, evaluated 32 at a time in a loop of arithmetic alone:
-// the same interactions as the per-visit walk, accumulated in list order (rounding may
-// differ from it in the last bits).  A cell stack that would overflow restarts the group
-// on the per-level walk (stack_cap entries: 256 by default, enough for every 64-body group
-// of the benchmarked spheres, which needed at most 99).
+// lane-parallel.  Each round the lanes take the children of up to four cells from the
+// group's cell stack, one child per lane (8 lanes per cell), and decide each child on its
+// own lane: a body is accepted; a cell is accepted when even the group's bounding box
+// passes the test (the box's distance components bound every body's from below, and the
+// rounded subtractions, the fused squares and the comparison are monotone, so every body's
+// own test passes), and opened when the group's body nearest the box centre fails it (then
+// the vote fails).  Only the remaining cells take the vote of every body, one after
+// another.  Accepted records go to a list in shared memory, evaluated 32 at a time in a
+// loop of arithmetic alone: the same interactions as the per-visit walk, accumulated in
+// list order (rounding may differ from it in the last bits).  A cell stack that would
+// overflow restarts the group on the per-level walk (stack_cap entries: 256 by default,
+// enough for every 64-body group of the benchmarked spheres, which needed at most 99).
 template <int W, bool REF, bool PB, bool FEAT, bool LIST = false>
 __device__ __forceinline__ void force_walk(const StepParams& p) {
     static_assert(!LIST || (W >= 32 && !REF), "the list walk takes whole-warp groups and FMA arithmetic");
