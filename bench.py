@@ -295,6 +295,8 @@ def _config(args, nbodies=None, counts=None):
          "error_samples": getattr(args, "error_samples", None)}
     if counts is not None:
         c.update({"universes": len(counts), "min_universe": int(min(counts)), "max_universe": int(max(counts))})
+    if getattr(args, "force_list", 0):
+        c["force_walk"] = "list" if args.force_list == 1 else "per-visit"
     return c
 
 
@@ -396,6 +398,9 @@ def main():
                     help="force launch geometry of a --profile-only run (0: the library default)")
     ap.add_argument("--stack-cap", type=int, default=0,
                     help="stack entries per vote group of a --profile-only run (0: the library default)")
+    ap.add_argument("--force-list", type=int, default=0, choices=(0, 1, 2),
+                    help="nbh_config.force_list: 1 the list walk, 2 the per-visit walk, 0 the library "
+                         "default (the list walk except in precise mode)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
@@ -436,7 +441,7 @@ def main():
 
     def new_sim(**kw):
         s_ = nbh.Simulation(theta=args.theta, eps=args.eps, dt=args.dt, device=local, precise=precise,
-                            vote_width=args.vote, **kw)
+                            vote_width=args.vote, force_list=args.force_list, **kw)
         if counts is None:
             s_.load(*arrs)
         else:

@@ -404,6 +404,37 @@ def test_precise_mode_matches_oracle():
         assert np.abs(gs[k] - os_[k]).max() <= 1e-5 * np.abs(os_[k]).max()
 
 
+def test_precise_mode_list_walk_option_keeps_the_interactions_and_the_error():
+    """Precise mode keeps the per-visit walk (the oracle's depth-first order of accumulation)
+    unless force_list = 1 asks for the list walk.  On a disc with a central point mass and a
+    halo (262,144 bodies, the 4M workload's generator) the list walk accepts the same nodes,
+    and its force error against the FP64 direct sum on sampled bodies has the same p99 and
+    median; the two sums differ by rounding order only (the central mass, whose acceleration
+    nearly cancels, is where they differ most)."""
+    import oracle as O
+    from nbh import universe as U
+    n = 1 << 18
+    arrs = U.DiscGalaxyGenerator(seed=31, rd=1.0, zd=0.1, center_mass=0.1, halo_frac=0.1).arrays(n)
+    idx = np.sort(np.random.default_rng(3).choice(n, 4096, replace=False)).astype(np.int32)
+    res = {}
+    for fl in (2, 1):
+        g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=64, precise=True, force_list=fl)
+        g.load(*arrs)
+        ref = g.direct_f64(idx)
+        g.step(1)
+        st = g.read()
+        err = O.rel_force_error(st["ax"][idx], st["ay"][idx], st["az"][idx], *ref)
+        res[fl] = (g.stats()["interactions"], g.tree()["sorted"], st, err)
+        g.close()
+    assert res[1][0] == res[2][0]
+    np.testing.assert_array_equal(res[1][1], res[2][1])
+    e1, e2 = res[1][3], res[2][3]
+    assert abs(np.percentile(e1, 99) / np.percentile(e2, 99) - 1) <= 1e-3
+    assert abs(np.median(e1) / np.median(e2) - 1) <= 1e-3
+    rel, _ = acc_rel(res[1][2], res[2][2])
+    assert np.median(rel) <= FMA_ACC_REL_MEDIAN, np.median(rel)
+
+
 def test_precise_mode_keeps_increments_below_an_ulp():
     """Two light bodies at x = +-1000 drifting at 1e-3 with dt = 1e-3: each step moves them
     1e-6, below half an FP32 ulp at 1000 (6.1e-5), so plain updates never move them while
