@@ -58,7 +58,7 @@ HBM_FALLBACK_GBS = 6800.0
 # DRAM bytes (read + write) of one force launch (vote width 64) on the 1,048,576-body
 # Plummer workload, from one full ncu capture of that launch (dram__bytes_read.sum +
 # dram__bytes_write.sum).
-FORCE_TRAFFIC_BYTES_1M = 218_074_368 + 24_569_856
+FORCE_TRAFFIC_BYTES_1M = 222_678_016 + 25_789_440
 
 # Algorithmic bytes per body / per cell of the memory-bound stages (minimum traffic:
 # every byte read and written once).
