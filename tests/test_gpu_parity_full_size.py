@@ -5,9 +5,11 @@ bodies; these reach the tree depths, stack depths and work-item counts of the be
 workloads:
 
 * the 1,048,576-body Plummer sphere (vote width 64, two steps so that the second one
-  applies the leapfrog velocity correction of calculateforce.cl:174-181), once with the
-  default shared-memory stack and once with a 64-entry stack, which walks trees deeper
-  than 9 levels with the per-level walk (calculateforce.cl:99-186) instead;
+  applies the leapfrog velocity correction of calculateforce.cl:174-181): the default list
+  walk; the per-visit walk with a 64-entry stack, which walks trees deeper than 9 levels
+  with the per-level walk (calculateforce.cl:99-186) in every group; and the list walk with
+  a 64-cell stack, which overflows for part of the groups and restarts them on the
+  per-level walk;
 * the ensemble of 256 Plummer universes, N per universe log-uniform in [1024, 65536]
   (3.59M bodies; 64-body work items that never straddle a universe);
 * the disc with a central point mass and a Plummer halo in precise mode (Kahan-compensated
@@ -58,17 +60,18 @@ def plummer_1m():
     return arrs, o.state(), o.tree_arrays()["sorted"], o.interactions, o.maxdepth
 
 
-@pytest.mark.parametrize("cap", [0, 64], ids=["shared-stack-walk", "per-level-walk"])
-def test_plummer_1m_matches_oracle(plummer_1m, cap):
+@pytest.mark.parametrize("cap,force_list", [(0, 0), (64, 2), (64, 1)],
+                         ids=["list-walk", "per-visit-per-level-walk", "list-walk-restarts"])
+def test_plummer_1m_matches_oracle(plummer_1m, cap, force_list):
     arrs, o_state, o_sorted, o_inter, o_depth = plummer_1m
-    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=64, stack_cap=cap)
+    g = gpu_sim(theta=0.5, eps=0.05, dt=0.01, vote_width=64, stack_cap=cap, force_list=force_list)
     g.load(*arrs)
     g.step(2)
-    if cap == 64:
+    if cap == 64 and force_list == 2:
         # a 64-entry stack covers (64 - 8) / 7 + 1 = 9 levels; this tree is deeper, so every
-        # group takes the per-level walk
+        # group of the per-visit walk takes the per-level walk
         assert o_depth > 9
-    _compare(g, o_state, o_sorted, o_inter, o_depth, "plummer 1M cap %d" % cap)
+    _compare(g, o_state, o_sorted, o_inter, o_depth, "plummer 1M cap %d walk %d" % (cap, force_list))
     g.close()
 
 
