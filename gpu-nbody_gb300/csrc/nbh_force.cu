@@ -80,8 +80,8 @@ __device__ __forceinline__ float dist2(const float dx, const float dy, const flo
 }
 
 // The first 32 records: unrolled completely for two or more bodies per lane (the 64-wide
-// walk's force 2.6 % faster than unrolled by 8), by 8 for one (the 32-wide walk measured
-// slower completely unrolled).
+// walk's force 2.6 % faster than unrolled by 8), by 8 for one (the 32-wide walk on a 16K
+// ball measured the same either way).
 template <int BPL, bool FEAT>
 __device__ __forceinline__ void eval_list32(const float4* lst, const float* lw, const float4 (&pb)[BPL],
                                             const float eps2, float (&ax)[BPL], float (&ay)[BPL], float (&az)[BPL],
